@@ -1,0 +1,365 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 photon walk: photons/s of the plain kernel on the
+2^30-photon workload (params.h optics: MU_A 2/cm, MU_S 20/cm, 101 shells of
+50 um, Philox seed 1, photon ids 0 .. 2^30-1).
+
+One step = one walk of the whole photon batch (one kernel launch).  Prints
+one JSON line (rank 0).  Usage:
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+* value: photons/s over all ranks, device time of the walk (CUDA events on
+  the launching stream), L2 flushed between timed steps;
+* e2e: the same metric through the C ABI's host-array call
+  tmc_photon_batch(heat, heat2, n, params), wall time of the whole call
+  (launch, walk, FP64 finalisation, device-to-host copy of the result);
+* roofline: the benchmark spec's bound of this path, SFU-class operations
+  (4 per photon step: log, 2 sqrt, divide) against the measured MUFU rate;
+* cpu_baseline: the reference's walk on this host's cores (libc rand).
+
+Multi-GPU (torchrun): each rank walks its own 2^30 photons (ids offset by
+rank), no collective on the data path; weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "photons/s on 1 GB300 (plain vs batched/served) at stated error; p50/p99 latency"
+UNIT = "photons/s"
+SFU_OPS_PER_STEP = 4          # log, sqrt (radius), divide + sqrt (direction)
+CPU_PHOTONS_PER_PROC = 1 << 16
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--photons", type=int, default=1 << 30)
+    ap.add_argument("--math", choices=["exact", "fast"], default="fast")
+    ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--blocks-per-sm", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(args, world):
+    return {
+        "workload": "plain walk, 2^30 photons per GPU (config 1)",
+        "photons_per_step_per_gpu": args.photons,
+        "shells": 101, "microns_per_shell": 50, "mu_a_per_cm": 2.0, "mu_s_per_cm": 20.0,
+        "rng": "Philox-4x32-10 keyed by photon id, seed 1",
+        "math": args.math,
+        "tallies": "u64 shared / u128 global fixed point (2^-40)",
+        "l2": "flushed between timed steps (256 MiB write); inputs are only parameters",
+        "parallelism": f"replicas x{world} (photon-id ranges)",
+    }
+
+
+# --------------------------------------------------------------- CPU side
+def _cpu_worker(args):
+    """One process: photons/s of the reference walk (libc rand) on one core."""
+    photons, seed = args
+    sys.path.insert(0, ROOT)
+    from oracle import oracle
+    if oracle.ref_available("cfg0", "nat"):
+        try:
+            L = oracle.ref_lib("cfg0", "nat")
+            return L.ref_native_rate(photons, seed), "reference"
+        except OSError:
+            pass
+    rate, _ = oracle.native_rate(oracle.cfg("cfg0"), photons, seed)
+    return rate, "port"
+
+
+class CpuPool:
+    def __init__(self, procs):
+        import multiprocessing as mp
+        self.procs = procs
+        self.pool = mp.get_context("spawn").Pool(procs)
+
+    def step(self, photons_per_proc):
+        t0 = time.perf_counter()
+        res = self.pool.map(_cpu_worker, [(photons_per_proc, i + 1) for i in range(self.procs)])
+        dt = time.perf_counter() - t0
+        kind = res[0][1]
+        return self.procs * photons_per_proc / dt, kind, [r[0] for r in res]
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline_measure():
+    from oracle import oracle
+    oracle.build(ref=False)
+    cores = cpu_cores()
+    pool = CpuPool(cores)
+    pool.step(1 << 12)                                    # warm the workers
+    rate, kind, per = pool.step(CPU_PHOTONS_PER_PROC * 2)
+    pool.close()
+    single = statistics.median(per)
+    return {
+        "value": rate, "unit": UNIT, "cores": cores, "kind": kind,
+        "single_thread_value": single,
+        "sample": f"{cores} processes x {CPU_PHOTONS_PER_PROC * 2} photons, params.h optics, "
+                  f"libc rand seeds 1..{cores} (one process per core); single-thread = median process",
+    }
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if rank != 0:
+        return 0
+    from oracle import oracle
+    oracle.build(ref=False)
+    cores = cpu_cores()
+    pool = CpuPool(cores)
+    for _ in range(args.warmup):
+        pool.step(CPU_PHOTONS_PER_PROC)
+    rates, times, kind = [], [], "port"
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r, kind, _ = pool.step(CPU_PHOTONS_PER_PROC)
+        times.append(time.perf_counter() - t0)
+        rates.append(r)
+    pool.close()
+    total = cores * CPU_PHOTONS_PER_PROC * args.steps
+    value = total / sum(times)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": workload_config(args, world), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": f"each step: {cores} processes x {CPU_PHOTONS_PER_PROC} photons of "
+                                   f"the reference walk (libc rand, params.h optics)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_id: str | None):
+        self.device_id = device_id
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        cmd = ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "200"]
+        if self.device_id:
+            cmd += ["-i", self.device_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+                power.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "power_w_max": max(power) if power else None,
+            "samples": len(sm),
+            "reasons": sorted(reasons),
+        }
+
+
+# ------------------------------------------------------------------- ours
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import tiny_mc_gb300 as tmc
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+
+    cpu_base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu_base = cpu_baseline_measure()
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    props = torch.cuda.get_device_properties(dev)
+    uuid = getattr(props, "uuid", None)
+    device_id = f"GPU-{uuid}" if uuid is not None else None
+
+    S = 101
+    p = tmc.params(seed=1, photon_id_base=rank * args.photons, math=args.math)
+    tmc.set_plain_launch(args.block, args.blocks_per_sm, 0)
+    tally = torch.zeros((S, 4), dtype=torch.int64, device=dev)
+    steps_ctr = torch.zeros(1, dtype=torch.int64, device=dev)
+    ws = torch.zeros(max(1, tmc.workspace_bytes() // 8), dtype=torch.int64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def one_step():
+        tmc.photon_batch_device(tally.data_ptr(), args.photons, p, steps_ctr.data_ptr(), ws.data_ptr(), sp)
+
+    sfu_peak = tmc.probe_sfu_rate()
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    steps_ctr.zero_()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    clocks = ClockSampler(device_id)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    t_wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        one_step()
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    if dist is not None:
+        dist.barrier()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(ms)
+    photon_steps = int(steps_ctr.item())
+    if dist is not None:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        ps = torch.tensor([photon_steps], device=dev, dtype=torch.int64)
+        dist.all_reduce(ps)
+        photon_steps_all = int(ps.item())
+    else:
+        photon_steps_all = photon_steps
+    photons_all = args.photons * args.steps * world
+    value = photons_all / (total_ms * 1e-3)
+
+    # roofline of the dominant kernel (the walk is the only kernel per step)
+    per_launch_s = (sum(ms) / len(ms)) * 1e-3
+    per_launch_ops = SFU_OPS_PER_STEP * photon_steps / args.steps
+    achieved = per_launch_ops / per_launch_s
+    roofline = {
+        "bound": "sfu", "achieved": achieved / 1e9, "peak": sfu_peak / 1e9, "unit": "Gop/s",
+        "frac": achieved / sfu_peak,
+        "traffic": None,
+        "algorithmic_unit": "4 SFU-class ops (log, sqrt, divide, sqrt) per photon step",
+        "photon_steps_per_launch": photon_steps / args.steps,
+        "peak_source": "measured live: MUFU lg2/sqrt/rcp probe (tmc_probe_sfu_rate)",
+    }
+
+    # e2e through the host-array C ABI call
+    e2e = None
+    if not args.no_e2e:
+        heat = np.zeros(S, np.float32)
+        heat2 = np.zeros(S, np.float32)
+        tmc.photon_batch(heat, heat2, args.photons, p)     # warm
+        if dist is not None:
+            dist.barrier()
+        wall = []
+        for _ in range(max(1, min(args.steps, 3))):
+            t0 = time.perf_counter()
+            tmc.photon_batch(heat, heat2, args.photons, p)
+            wall.append(time.perf_counter() - t0)
+        tw = sum(wall)
+        if dist is not None:
+            t = torch.tensor([tw], dtype=torch.float64, device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tw = float(t.item())
+        e2e = {"value": args.photons * len(wall) * world / tw, "unit": UNIT,
+               "h2d_bytes_per_step": 40, "d2h_bytes_per_step": 16 * S,
+               "call": "tmc_photon_batch(heat, heat2, n, params) with host float arrays"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(args, world),
+            "photon_steps_per_s": photon_steps_all / (total_ms * 1e-3),
+            "steps_per_photon": photon_steps_all / photons_all,
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu_base,
+            "gpu_launches": args.steps, "clocks": clk, "wall_s_timed_region": t_wall,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,155 @@
+/*
+ * tmc.h — C ABI of libtmc_gb300.so, the GB300 (sm_103a) photon walk of
+ * Tiny Monte Carlo (computacionparalela/tiny_mc).
+ *
+ * The reference's boundary is one call per photon,
+ *     void photon(float *heats, float *heats_squared);        photon.h:3
+ * with compile-time knobs (params.h:5-27) and the global libc rand() seeded by
+ * the caller (tiny_mc.c:43).  This library replaces the caller's photon loop
+ * (tiny_mc.c:47-49) by ONE call that walks n photons on the GPU and
+ * accumulates (+=) into the same two caller-owned float arrays.
+ *
+ * Plain pointers and sizes only; no CUDA or torch types in the signatures
+ * (streams are passed as void*, a cudaStream_t or NULL for the default
+ * stream).  All entry points return TMC_OK (0) or a negative tmc_status.
+ *
+ * Thread safety: like photon() (global rand, unsynchronised +=), the library
+ * is meant to be driven by one host thread at a time per process; calls are
+ * serialised by an internal lock so concurrent calls are safe but not
+ * concurrent.
+ */
+#ifndef TMC_H
+#define TMC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TMC_ABI_VERSION 1
+
+typedef enum tmc_status {
+    TMC_OK = 0,
+    TMC_E_INVALID = -1,   /* a parameter is out of range (e.g. mu_a <= 0, shells == 0) */
+    TMC_E_CUDA = -2,      /* a CUDA runtime call failed; tmc_last_error() has the text */
+    TMC_E_NOMEM = -3,     /* device or host allocation failed */
+    TMC_E_TIMEOUT = -4,   /* a bounded device-side or host-side wait ran out */
+    TMC_E_OVERFLOW = -5,  /* a count would overflow its integer type */
+    TMC_E_NODEVICE = -6,  /* no CUDA device, or not an sm_103 device */
+    TMC_E_BUSY = -7,      /* admission refused (served mode: no slot or tally memory) */
+    TMC_E_STATE = -8      /* call not valid in the current state (e.g. unknown request id) */
+} tmc_status;
+
+/* Arithmetic of the walk. */
+typedef enum tmc_math {
+    /* Every float operation of photon.c:21-49 IEEE-rounded in photon.c's
+     * order (no FMA contraction), sqrtf and divisions correctly rounded, and
+     * the step-length logarithm evaluated by the library's own fixed sequence
+     * of float operations.  Integer tallies are bit-identical to the CPU
+     * restatement of photon.c driven by the same Philox streams. */
+    TMC_MATH_EXACT = 0,
+    /* Hardware approximations: lg2.approx for the logarithm, sqrt.approx,
+     * contracted multiply-adds and (1-u^2)/t rewritten as 4(1-t).  Same draws
+     * and branch decisions; tallies agree with the exact form statistically
+     * (per-shell relative differences far below 1e-4 at config-1 optics). */
+    TMC_MATH_FAST = 1
+} tmc_math;
+
+/* Runtime form of params.h's knobs. */
+typedef struct tmc_params {
+    uint32_t shells;            /* SHELLS            (params.h:5-7),   >= 1      */
+    float microns_per_shell;    /* MICRONS_PER_SHELL (params.h:21-23), > 0       */
+    float mu_a;                 /* MU_A, 1/cm        (params.h:13-15), > 0       */
+    float mu_s;                 /* MU_S, 1/cm        (params.h:17-19), >= 0      */
+    uint64_t seed;              /* SEED (params.h:25-27): the Philox key          */
+    uint64_t photon_id_base;    /* photon ids of this call: base .. base+n-1      */
+    uint32_t math;              /* tmc_math                                        */
+    uint32_t reserved;          /* must be 0                                       */
+} tmc_params;
+
+/*
+ * Exact per-shell tallies.  A deposit of weight w (photon.c:30-31 deposits
+ * (1-albedo)*w) adds rint(w * 2^40) to sum_w and rint(fl(w*w) * 2^40) to
+ * sum_w2, as 128-bit unsigned integers split in 64-bit halves.  Integer sums
+ * make results independent of thread order: runs are bit-reproducible.
+ *   heat[s]  = (1-albedo)   * sum_w  * 2^-40
+ *   heat2[s] = (1-albedo)^2 * sum_w2 * 2^-40
+ */
+typedef struct tmc_tally {
+    uint64_t w_lo, w_hi;
+    uint64_t w2_lo, w2_hi;
+} tmc_tally;
+
+/* params.h defaults: SHELLS 101, MICRONS_PER_SHELL 50, MU_A 2, MU_S 20;
+ * seed 1, photon_id_base 0, TMC_MATH_EXACT. */
+void tmc_params_default(tmc_params *p);
+
+/*
+ * The drop-in for the photon loop of tiny_mc.c:47-49 (one photon() call per
+ * photon, photon.c:6).  Walks photons photon_id_base .. +n_photons-1 and
+ * ACCUMULATES into caller-owned host arrays of length p->shells:
+ *     heat[s]  += (1-albedo) * sum of w      over deposits in shell s
+ *     heat2[s] += (1-albedo)^2 * sum of w^2  over deposits in shell s
+ * heat2 keeps photon.c:31's per-deposit-square meaning.  Synchronous.
+ */
+int tmc_photon_batch(float *heat, float *heat2, uint64_t n_photons, const tmc_params *p);
+
+/* Same walk; adds the exact integer tallies into host `tally` [p->shells].
+ * photon_steps (may be NULL) += number of deposits (= photon steps). */
+int tmc_photon_batch_fx(tmc_tally *tally, uint64_t n_photons, const tmc_params *p,
+                        uint64_t *photon_steps);
+
+/* Bytes of device scratch the device-pointer entry points need. */
+size_t tmc_workspace_bytes(void);
+
+/*
+ * Device-resident form: d_tally is DEVICE memory [p->shells] and is added to
+ * (+=).  d_steps (device, may be NULL) += photon steps.  d_workspace is
+ * device scratch of tmc_workspace_bytes() bytes, or NULL to use a buffer the
+ * library allocates once per device.  stream is a cudaStream_t (NULL =
+ * legacy default stream).  Asynchronous: returns after the launch.
+ */
+int tmc_photon_batch_device(tmc_tally *d_tally, uint64_t n_photons, const tmc_params *p,
+                            uint64_t *d_steps, void *d_workspace, void *stream);
+
+/* FP64 conversion of exact tallies (host arrays): heat/heat2 as defined at
+ * tmc_tally.  Either output may be NULL. */
+int tmc_tally_to_heat(const tmc_tally *tally, const tmc_params *p, double *heat, double *heat2);
+
+/*
+ * The report of tiny_mc.c:58-66, from float heat/heat2 of `photons` photons:
+ * the two column-title lines, one line per shell but the last, and the
+ * "# extra" line, with the same printf formats and the same float/double
+ * arithmetic.  Writes at most cap bytes (NUL-terminated); returns the length
+ * it needed (excluding NUL), or a negative tmc_status.
+ */
+int tmc_format_report(char *buf, size_t cap, const float *heat, const float *heat2,
+                      uint64_t photons, const tmc_params *p);
+
+/*
+ * Launch shape of the plain walk: threads per block (128, 256 or 512; 0 =
+ * default), resident blocks per SM (0 = occupancy limit) and a cap on the
+ * grid (0 = none).  Results do not depend on it (integer tallies,
+ * photon-keyed streams); only speed does.
+ */
+int tmc_set_plain_launch(int block, int blocks_per_sm, int max_blocks);
+
+/* The first n rand() values of photon `photon` under `seed`, produced by the
+ * device's Philox path (one small kernel); out is a host array of n int32. */
+int tmc_debug_rand(uint64_t seed, uint64_t photon, uint32_t n, int32_t *out);
+
+/* Measured throughput of the special-function unit on the current device
+ * (lg2/sqrt/rcp approximations, MUFU ops per second over all SMs): the
+ * denominator of the walk's SFU roofline.  No reference counterpart. */
+int tmc_probe_sfu_rate(double *mufu_ops_per_s);
+
+/* Text of a status code, and the last CUDA error message seen. */
+const char *tmc_strerror(int status);
+const char *tmc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TMC_H */

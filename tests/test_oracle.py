@@ -1,0 +1,170 @@
+"""The CPU oracle pinned against the reference (no GPU needed).
+
+The reference has no tests of its own (no golden files, no test target); the
+pins here are outputs of the reference itself, recorded by
+tests/golden/make_golden.py, plus live comparisons with oracle/_ref/ (the
+reference's sources compiled unchanged) where the reference tree exists.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ref_tree_available
+
+GOLD_NATIVE = os.path.join(GOLDEN, "ref_native.npz")
+GOLD_INJ = os.path.join(GOLDEN, "ref_injected.npz")
+GOLD_STDOUT = os.path.join(GOLDEN, "ref_cfg0_seed1_stdout.txt")
+
+
+# ------------------------------------------------------------------ Philox
+def test_philox_structure(oracle_mod):
+    """Counter-based: distinct counters/keys give distinct blocks; stream
+    word n of photon p is word n%4 of block n/4 (counter {n/4, 0, p, p>>32})."""
+    o = oracle_mod
+    a = o.philox([0, 0, 0, 0], [0, 0])
+    b = o.philox([1, 0, 0, 0], [0, 0])
+    c = o.philox([0, 0, 0, 0], [1, 0])
+    assert not np.array_equal(a, b) and not np.array_equal(a, c)
+    s = o.stream(7, 12345, 12)
+    for blk in range(3):
+        words = o.philox([blk, 0, 12345, 0], [7, 0])
+        r = np.maximum(words >> 1, 1).astype(np.int32)
+        assert np.array_equal(s[4 * blk:4 * blk + 4], r)
+    hi = o.stream(7, (3 << 32) | 5, 4)
+    words = o.philox([0, 0, 5, 3], [7, 0])
+    assert np.array_equal(hi, np.maximum(words >> 1, 1).astype(np.int32))
+
+
+def test_rand_range_and_zero_mapping(oracle_mod):
+    s = oracle_mod.stream(1, 0, 1 << 16)
+    assert s.min() >= 1 and s.max() <= (1 << 31) - 1
+    # uniformity sanity: mean of U = r/2^31 close to 1/2
+    u = s.astype(np.float64) / 2 ** 31
+    assert abs(u.mean() - 0.5) < 0.01
+
+
+# -------------------------------------------------------------------- log
+def test_tmo_logf_accuracy(oracle_mod):
+    rng = np.random.default_rng(0)
+    r = rng.integers(1, 2 ** 31, 20000)
+    xs = (r.astype(np.float32) / np.float32(2 ** 31)).astype(np.float32)
+    xs = np.concatenate([xs, np.float32([1.0, 0.5, 2.0 ** -31, np.nextafter(np.float32(1), np.float32(0))])])
+    worst = 0.0
+    for x in xs:
+        v = oracle_mod.logf(float(x))
+        ref = np.log(np.float64(x))
+        if ref == 0.0:
+            assert v == 0.0
+            continue
+        worst = max(worst, abs(v - ref) / float(np.spacing(np.float32(abs(ref)))))
+    assert worst < 2.0
+
+
+# ------------------------------------------- restatement vs reference photon.c
+@pytest.mark.parametrize("name", ["cfg0", "cfg2"])
+@pytest.mark.parametrize("log_mode", [0, 1])
+def test_restatement_matches_reference_photon_golden(oracle_mod, name, log_mode):
+    """Per-photon float arrays of the FP32 restatement are bit-identical to
+    the reference's own photon() fed the same Philox stream (golden hashes)."""
+    g = np.load(GOLD_INJ)
+    ref_hashes = g[f"{name}_log{log_mode}_hashes"]
+    hashes, hs, h2s = oracle_mod.photon_hashes(oracle_mod.cfg(name), len(ref_hashes),
+                                               log_mode=log_mode)
+    assert np.array_equal(hashes, ref_hashes)
+    assert np.array_equal(hs, g[f"{name}_log{log_mode}_heat"])
+    assert np.array_equal(h2s, g[f"{name}_log{log_mode}_heat2"])
+
+
+@pytest.mark.skipif(not ref_tree_available(), reason="reference tree not present")
+@pytest.mark.parametrize("name,n,base", [("cfg0", 300, 1 << 33), ("cfg2", 8, 977)])
+def test_restatement_matches_reference_photon_live(oracle_mod, name, n, base):
+    oracle_mod.build(ref=True)
+    for log_mode in (0, 1):
+        a = oracle_mod.photon_hashes(oracle_mod.cfg(name, seed=99), n, id_base=base, log_mode=log_mode)
+        b = oracle_mod.ref_photon_hashes(name, n, seed=99, id_base=base, log_mode=log_mode)
+        assert np.array_equal(a[0], b[0])
+
+
+def test_native_replay_matches_reference_arrays(oracle_mod):
+    """libc-rand replay == the reference's float arrays after srand(1), bitwise."""
+    g = np.load(GOLD_NATIVE)
+    for name in ("cfg0", "cfg2"):
+        n, batch = int(g[f"{name}_n"]), int(g[f"{name}_batch"])
+        h, h2, bh, bh2 = oracle_mod.native_run(oracle_mod.cfg(name), n, 1, batch=batch)
+        assert np.array_equal(h.view(np.uint32), g[f"{name}_heat"].view(np.uint32))
+        assert np.array_equal(h2.view(np.uint32), g[f"{name}_heat2"].view(np.uint32))
+        assert np.array_equal(bh.view(np.uint32), g[f"{name}_bheat"].view(np.uint32))
+        assert np.array_equal(bh2.view(np.uint32), g[f"{name}_bheat2"].view(np.uint32))
+
+
+def test_golden_stdout_md5():
+    import hashlib
+    with open(GOLD_STDOUT, "rb") as f:
+        assert hashlib.md5(f.read()).hexdigest() == "efbe7df98bd29007f10f4ac5d1e530db"
+
+
+# ------------------------------------------------ fixed-point tallies, FP64
+def test_fx_tallies_consistent_with_float_walk(oracle_mod):
+    """Exact tallies of the restatement against its per-photon float arrays:
+    (1-a)*sum_w matches photon.c:30's float sums to float rounding."""
+    o = oracle_mod
+    p = o.cfg("cfg0")
+    n = 2000
+    tally, dep, steps = o.walk_fx(p, n, nthreads=2)
+    heat, heat2 = o.heat_from_tally(p, tally)
+    _, hs, h2s = o.photon_hashes(p, n)
+    m = dep > 100
+    assert np.allclose(heat[m], hs[m], rtol=2e-6)
+    assert np.allclose(heat2[m], h2s[m], rtol=2e-5)
+    assert steps == int(dep.sum())
+
+
+def test_fx_thread_split_invariance(oracle_mod):
+    o = oracle_mod
+    p = o.cfg("cfg0", seed=5)
+    a = o.walk_fx(p, 3000, id_base=17, nthreads=1)
+    b = o.walk_fx(p, 3000, id_base=17, nthreads=7)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2]
+    # splitting the id range across two calls and adding gives the same sums
+    c1 = o.walk_fx(p, 1000, id_base=17)
+    c2 = o.walk_fx(p, 2000, id_base=1017)
+    s = [int(a[0][i, 1]) << 64 | int(a[0][i, 0]) for i in range(p.shells)]
+    t = [(int(c1[0][i, 1]) << 64 | int(c1[0][i, 0])) + (int(c2[0][i, 1]) << 64 | int(c2[0][i, 0]))
+         for i in range(p.shells)]
+    assert s == t
+
+
+def test_fp32_vs_fp64_oracle_cfg0(oracle_mod):
+    """The FP32 walk (photon.c arithmetic) agrees with the FP64 oracle to 1e-4
+    in every shell with >= 1e4 deposits at params.h optics."""
+    o = oracle_mod
+    p = o.cfg("cfg0")
+    n = 1 << 16
+    tally, dep, _ = o.walk_fx(p, n, log_mode=o.LOG_NATIVE)
+    h32, _ = o.heat_from_tally(p, tally)
+    h64, _, dep64 = o.walk_f64(p, n)
+    m = dep >= 10000
+    assert m.sum() > 50
+    rel = np.abs(h32[m] - h64[m]) / h64[m]
+    assert rel.max() < 1e-4
+
+
+def test_oracle_stat_vs_native_reference(oracle_mod):
+    """Philox-driven restatement vs the reference's libc-rand run (seed 1):
+    per-shell |z| <= 4 with batch-means sigma on both sides."""
+    o = oracle_mod
+    g = np.load(GOLD_NATIVE)
+    p = o.cfg("cfg0")
+    ref_b = g["cfg0_bheat"].astype(np.float64)      # 32 batches x 1024 photons
+    nb, per = 64, 2048
+    means = []
+    for b in range(nb):
+        t, _, _ = o.walk_fx(p, per, id_base=b * per)
+        means.append(o.heat_from_tally(p, t)[0] / per)
+    means = np.array(means)
+    ref_means = ref_b / int(g["cfg0_batch"])
+    mu_a, se_a = means.mean(0), means.std(0, ddof=1) / np.sqrt(nb)
+    mu_b, se_b = ref_means.mean(0), ref_means.std(0, ddof=1) / np.sqrt(len(ref_means))
+    z = (mu_a - mu_b) / np.sqrt(se_a ** 2 + se_b ** 2)
+    assert np.all(np.abs(z[:-1]) < 4.0), np.abs(z).max()

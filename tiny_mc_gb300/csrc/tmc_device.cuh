@@ -1,0 +1,205 @@
+// tmc_device.cuh — device building blocks of the photon walk (sm_103a).
+//
+// Reference: computacionparalela/tiny_mc photon.c:6-51 (one photon per call,
+// global libc rand()).  Here one thread carries one photon at a time; the
+// random numbers come from a Philox-4x32-10 stream keyed by the photon id, so
+// the walk of photon p is the same whichever thread, warp or launch runs it.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "tmc.h"
+
+namespace tmc {
+
+constexpr unsigned FULL_MASK = 0xffffffffu;
+
+// ----------------------------------------------------------------- Philox
+// Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).  The ten round keys
+// depend only on the seed, so they are precomputed on the host and passed in
+// the kernel parameter block: every XOR with a key then reads the constant
+// bank instead of spending an add per round.
+constexpr uint32_t PHILOX_M0 = 0xD2511F53u;
+constexpr uint32_t PHILOX_M1 = 0xCD9E8D57u;
+constexpr uint32_t PHILOX_W0 = 0x9E3779B9u;
+constexpr uint32_t PHILOX_W1 = 0xBB67AE85u;
+
+struct PhiloxKeys {
+    uint32_t k0[10];
+    uint32_t k1[10];
+};
+
+inline PhiloxKeys make_philox_keys(uint64_t seed)
+{
+    PhiloxKeys k;
+    uint32_t a = (uint32_t)seed, b = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        k.k0[r] = a;
+        k.k1[r] = b;
+        a += PHILOX_W0;
+        b += PHILOX_W1;
+    }
+    return k;
+}
+
+// Counter {c0, c1, c2, c3} -> four 32-bit words.
+__device__ __forceinline__ uint4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                               const PhiloxKeys &K)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const unsigned long long p0 = (unsigned long long)PHILOX_M0 * c0;
+        const unsigned long long p1 = (unsigned long long)PHILOX_M1 * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ K.k0[r];
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ K.k1[r];
+        c1 = (uint32_t)p1;
+        c3 = (uint32_t)p0;
+        c0 = n0;
+        c2 = n2;
+    }
+    return make_uint4(c0, c1, c2, c3);
+}
+
+// rand() of photon.c: 31 bits of a Philox word; 0 becomes 1 so that
+// -log(rand()/RAND_MAX) is always finite (the reference's logf(0) case).
+__device__ __forceinline__ uint32_t rand31(uint32_t word)
+{
+    return max(word >> 1, 1u);
+}
+
+// rand()/(float)RAND_MAX: (float)RAND_MAX is exactly 2^31, so the quotient is
+// the correctly rounded int->float conversion scaled by 2^-31 (exact).
+__device__ __forceinline__ float uniform01(uint32_t word)
+{
+    return __uint2float_rn(rand31(word)) * 0x1p-31f;
+}
+
+// 2.0f*rand()/(float)RAND_MAX - 1.0f: 2*fl(r)/2^31 is exact, so one fused
+// multiply-add rounds exactly once where photon.c rounds once (the "- 1").
+__device__ __forceinline__ float uniform_pm1(uint32_t word)
+{
+    return fmaf(__uint2float_rn(rand31(word)), 0x1p-30f, -1.0f);
+}
+
+// ------------------------------------------------------------ arithmetic
+// The library's logarithm for TMC_MATH_EXACT: x = 2^k m, m in
+// [sqrt(1/2), sqrt(2)); log(m) = 2 atanh(s), s = (m-1)/(m+1), odd Taylor
+// series of atanh through s^9; log x = k ln2_hi + (k ln2_lo + log m).  Each
+// step is one IEEE-rounded float operation (no contraction), so the CPU
+// restatement reproduces it bit for bit.  Max error about 1.6 ulp on
+// [2^-31, 1].
+__device__ __forceinline__ float log_exact(float x)
+{
+    const uint32_t ix = __float_as_uint(x);
+    const int k = (int)((ix + 0x004afb0du) >> 23) - 127;
+    const float m = __uint_as_float(ix - ((uint32_t)k << 23));
+    const float f = __fsub_rn(m, 1.0f);
+    const float s = __fdiv_rn(f, __fadd_rn(2.0f, f));
+    const float z = __fmul_rn(s, s);
+    float pz = 0.222222222f;                          // 2/9
+    pz = __fadd_rn(__fmul_rn(pz, z), 0.285714286f);   // 2/7
+    pz = __fadd_rn(__fmul_rn(pz, z), 0.4f);           // 2/5
+    pz = __fadd_rn(__fmul_rn(pz, z), 0.666666667f);   // 2/3
+    const float tail = __fmul_rn(__fmul_rn(s, z), pz);
+    const float lm = __fadd_rn(__fadd_rn(s, s), tail);
+    const float kf = (float)k;
+    const float hi = __fmul_rn(kf, 0.693145751953125f);
+    const float lo = __fmul_rn(kf, 1.42860682e-6f);
+    return __fadd_rn(hi, __fadd_rn(lo, lm));
+}
+
+__device__ __forceinline__ float sqrt_approx(float x)
+{
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// photon.c's float expressions, IEEE-rounded one operation at a time.
+struct ExactMath {
+    static constexpr uint32_t id = TMC_MATH_EXACT;
+    // -logf(U), photon.c:21
+    __device__ static __forceinline__ float step_length(float U) { return -log_exact(U); }
+    // x += t * u, photon.c:22-24
+    __device__ static __forceinline__ float move(float x, float t, float u)
+    {
+        return __fadd_rn(x, __fmul_rn(t, u));
+    }
+    // sqrtf(x*x + y*y + z*z) * shells_per_mfp, photon.c:26
+    __device__ static __forceinline__ float radius_shells(float x, float y, float z, float spm)
+    {
+        const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
+        return __fmul_rn(__fsqrt_rn(r2), spm);
+    }
+    // xi1*xi1 + xi2*xi2, photon.c:39
+    __device__ static __forceinline__ float norm2(float a, float b)
+    {
+        return __fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b));
+    }
+    // sqrtf((1.0f - u*u) / t), photon.c:42-43
+    __device__ static __forceinline__ float dir_scale(float t, float u)
+    {
+        return __fsqrt_rn(__fdiv_rn(__fsub_rn(1.0f, __fmul_rn(u, u)), t));
+    }
+    __device__ static __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+};
+
+// Hardware approximations (MUFU lg2 / sqrt), contraction allowed.
+struct FastMath {
+    static constexpr uint32_t id = TMC_MATH_FAST;
+    __device__ static __forceinline__ float step_length(float U) { return -__logf(U); }
+    __device__ static __forceinline__ float move(float x, float t, float u) { return fmaf(t, u, x); }
+    __device__ static __forceinline__ float radius_shells(float x, float y, float z, float spm)
+    {
+        return sqrt_approx(fmaf(x, x, fmaf(y, y, z * z))) * spm;
+    }
+    __device__ static __forceinline__ float norm2(float a, float b) { return fmaf(a, a, b * b); }
+    // (1-u^2)/t with u = 2t-1 is 4(1-t): sqrt of it is 2 sqrt(1-t)
+    __device__ static __forceinline__ float dir_scale(float t, float)
+    {
+        return 2.0f * sqrt_approx(1.0f - t);
+    }
+    __device__ static __forceinline__ float mul(float a, float b) { return a * b; }
+};
+
+// ---------------------------------------------------------------- tallies
+// Fixed point of a deposit weight: rint(w * 2^40).  w <= 1, so one deposit
+// is at most 2^40 units.
+__device__ __forceinline__ unsigned long long fx40(float w)
+{
+    return __float2ull_rn(w * 0x1p40f);
+}
+
+// Add v to a 64-bit shared-memory tally; when the 64-bit sum wraps, carry
+// 2^64 units into the 128-bit global tally's high word.  The global word
+// receives only carries until the final flush, so no epoch barriers are
+// needed however many photons a block walks.
+__device__ __forceinline__ void add_carry(unsigned long long *sh, unsigned long long *g_hi,
+                                          unsigned long long v)
+{
+    const unsigned long long old = atomicAdd(sh, v);
+    if (old + v < old)
+        atomicAdd(g_hi, 1ull);
+}
+
+// Flush a 64-bit partial sum into a 128-bit global tally.
+__device__ __forceinline__ void flush128(unsigned long long *g_lo, unsigned long long *g_hi,
+                                         unsigned long long v)
+{
+    if (v) {
+        const unsigned long long old = atomicAdd(g_lo, v);
+        if (old + v < old)
+            atomicAdd(g_hi, 1ull);
+    }
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(FULL_MASK, v, o);
+    return v;
+}
+
+}  // namespace tmc
