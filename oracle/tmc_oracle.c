@@ -143,6 +143,8 @@ static int derive32(const tmo_params *p, derived32 *d)
     d->spm = (float)(1e4 / (double)p->microns_per_shell / (double)(p->mu_a + p->mu_s));
     d->c = 1.0f - d->albedo;
     d->shells = p->shells;
+    if (!(d->albedo < 1.0f))   /* weight would never decay: no photon would die */
+        return -1;
     return 0;
 }
 

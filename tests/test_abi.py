@@ -43,6 +43,7 @@ def test_params_default_is_params_h(tmc_mod):
 @pytest.mark.parametrize("field,value", [
     ("shells", 0), ("mu_a", 0.0), ("mu_a", -1.0), ("mu_a", float("nan")), ("mu_s", -1.0),
     ("mu_s", float("inf")), ("microns_per_shell", 0.0), ("math", 7), ("reserved", 1),
+    ("mu_a", 1e-9),   # float albedo rounds to 1: the weight would never decay
 ])
 def test_invalid_params_rejected_before_any_launch(tmc_mod, field, value):
     p = tmc_mod.params()

@@ -54,6 +54,10 @@ int validate(const tmc_params *p)
         return TMC_E_INVALID;
     if (p->reserved != 0)
         return TMC_E_INVALID;
+    // If mu_a is so small against mu_s that the float albedo rounds to 1, the
+    // weight never decays (photon.c:32) and no photon would ever die.
+    if (!(p->mu_s / (p->mu_s + p->mu_a) < 1.0f))
+        return TMC_E_INVALID;
     return TMC_OK;
 }
 

@@ -164,22 +164,32 @@ struct FastMath {
 };
 
 // ---------------------------------------------------------------- tallies
-// Fixed point of a deposit weight: rint(w * 2^40).  w <= 1, so one deposit
-// is at most 2^40 units.
-__device__ __forceinline__ unsigned long long fx40(float w)
+// Fixed point of a deposit weight: rint(w * 2^40), returned as 32-bit halves,
+// for 0 <= w <= 1 (a deposit is at most 2^40 units).  hi = floor(w * 2^8);
+// the remainder w*2^40 - hi*2^32 is exact in one fused multiply-add (it is
+// the low part of w's own significand), and its correctly rounded conversion
+// is the low word: exact for w >= 2^-17, where w*2^40 is an integer, and
+// round-to-nearest-even below.  No branch, and no float->u64 conversion (that
+// one runs on the FP64 pipe).
+__device__ __forceinline__ void fx40_split(float w, uint32_t &lo, uint32_t &hi)
 {
-    return __float2ull_rn(w * 0x1p40f);
+    hi = __float2uint_rz(w * 0x1p8f);
+    const float rem = fmaf(-__uint2float_rn(hi), 0x1p32f, w * 0x1p40f);
+    lo = __float2uint_rn(rem);
 }
 
-// Add v to a 64-bit shared-memory tally; when the 64-bit sum wraps, carry
-// 2^64 units into the 128-bit global tally's high word.  The global word
-// receives only carries until the final flush, so no epoch barriers are
-// needed however many photons a block walks.
-__device__ __forceinline__ void add_carry(unsigned long long *sh, unsigned long long *g_hi,
-                                          unsigned long long v)
+// Add (hi:lo) to a 64-bit shared-memory tally kept as two 32-bit words, with
+// native 32-bit shared atomics: the carry out of the low word goes into the
+// high word, and a wrap of the high word carries 2^64 units into the 128-bit
+// global tally.  The global word receives only such carries until the final
+// flush, so no epoch barriers are needed however many photons a block walks.
+__device__ __forceinline__ void tally_add(uint32_t *sh_lo, uint32_t *sh_hi,
+                                          unsigned long long *g_hi, uint32_t lo, uint32_t hi)
 {
-    const unsigned long long old = atomicAdd(sh, v);
-    if (old + v < old)
+    const uint32_t old = atomicAdd(sh_lo, lo);
+    hi += (old + lo < old) ? 1u : 0u;
+    const uint32_t oh = atomicAdd(sh_hi, hi);
+    if (oh + hi < oh)
         atomicAdd(g_hi, 1ull);
 }
 
