@@ -114,6 +114,25 @@ size_t tmc_workspace_bytes(void);
 int tmc_photon_batch_device(tmc_tally *d_tally, uint64_t n_photons, const tmc_params *p,
                             uint64_t *d_steps, void *d_workspace, void *stream);
 
+/*
+ * Allocation-free form of tmc_photon_batch (same walk, same result, host
+ * arrays).  No counterpart in the reference: photon() never touches device
+ * memory.  For callers that cannot let a library call cudaMalloc — device
+ * memory owned by another allocator, or a loop that forbids allocation after
+ * start-up.  Its device scratch (claim counter, tallies, FP64 results) is a
+ * fixed array of TMC_STATIC_SCRATCH_BYTES inside the library, held by every
+ * GPU that loads the library until the process exits.  shells above
+ * TMC_STATIC_MAX_SHELLS return TMC_E_INVALID.  The first call on a device
+ * looks up that array's device address; make it before any stream capture.
+ * All calls share the array (each clears what it uses first); calls are
+ * serialised and synchronous, and two of them running at once on the GPU
+ * would race.  stream: a cudaStream_t or NULL.
+ */
+#define TMC_STATIC_MAX_SHELLS 4096
+#define TMC_STATIC_SCRATCH_BYTES (256 + 32 * TMC_STATIC_MAX_SHELLS + 16 * TMC_STATIC_MAX_SHELLS)
+int tmc_photon_batch_static(float *heat, float *heat2, uint64_t n_photons, const tmc_params *p,
+                            void *stream);
+
 /* FP64 conversion of exact tallies (host arrays): heat/heat2 as defined at
  * tmc_tally.  Either output may be NULL. */
 int tmc_tally_to_heat(const tmc_tally *tally, const tmc_params *p, double *heat, double *heat2);

@@ -88,6 +88,8 @@ def lib() -> ctypes.CDLL:
         L.tmc_set_plain_launch.restype = i32
         L.tmc_debug_rand.argtypes = [u64, u64, ctypes.c_uint32, vp]
         L.tmc_debug_rand.restype = i32
+        L.tmc_photon_batch_static.argtypes = [vp, vp, u64, P, vp]
+        L.tmc_photon_batch_static.restype = i32
         L.tmc_probe_sfu_rate.argtypes = [vp]
         L.tmc_probe_sfu_rate.restype = i32
         L.tmc_strerror.argtypes = [i32]
@@ -124,6 +126,20 @@ def photon_batch(heat: np.ndarray, heat2: np.ndarray, n_photons: int, p: Params)
     _f32(heat2, p.shells, "heat2")
     _check(lib().tmc_photon_batch(heat.ctypes.data, heat2.ctypes.data, n_photons, ctypes.byref(p)),
            "tmc_photon_batch")
+
+
+STATIC_MAX_SHELLS = 4096
+
+
+def photon_batch_static(heat: np.ndarray, heat2: np.ndarray, n_photons: int, p: Params,
+                        stream: int = 0) -> None:
+    """photon_batch for callers that cannot let the library allocate device
+    memory: its scratch is a fixed array inside the library (shells <= 4096)."""
+    _f32(heat, p.shells, "heat")
+    _f32(heat2, p.shells, "heat2")
+    _check(lib().tmc_photon_batch_static(heat.ctypes.data, heat2.ctypes.data, n_photons,
+                                         ctypes.byref(p), stream or None),
+           "tmc_photon_batch_static")
 
 
 def photon_batch_fx(n_photons: int, p: Params, tally: np.ndarray | None = None):
