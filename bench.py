@@ -38,6 +38,10 @@ METRIC = "photons/s on 1 GB300 (plain vs batched/served) at stated error; p50/p9
 UNIT = "photons/s"
 SFU_OPS_PER_STEP = 4          # log, sqrt (radius), divide + sqrt (direction)
 CPU_PHOTONS_PER_PROC = 1 << 16
+# DRAM bytes (read + write) of one walk launch, from an ncu capture of the walk
+# at config-1 optics (2^25 photons): only the 101-shell tally flush touches
+# DRAM, so the figure does not grow with the photon count.
+WALK_DRAM_BYTES_PER_LAUNCH = 19968
 
 
 def parse():
@@ -309,11 +313,26 @@ def run_ours(args):
     roofline = {
         "bound": "sfu", "achieved": achieved / 1e9, "peak": sfu_peak / 1e9, "unit": "Gop/s",
         "frac": achieved / sfu_peak,
-        "traffic": None,
+        "traffic": WALK_DRAM_BYTES_PER_LAUNCH,
+        "traffic_note": "DRAM bytes per launch (ncu); tally flush only, independent of photons",
         "algorithmic_unit": "4 SFU-class ops (log, sqrt, divide, sqrt) per photon step",
         "photon_steps_per_launch": photon_steps / args.steps,
         "peak_source": "measured live: MUFU lg2/sqrt/rcp probe (tmc_probe_sfu_rate)",
     }
+
+    # the exact (bit-reproducible) arithmetic on the same workload, for reference
+    value_exact = None
+    if args.math == "fast" and not args.no_e2e:
+        pe = tmc.params(seed=1, photon_id_base=rank * args.photons, math="exact")
+        tmc.photon_batch_device(tally.data_ptr(), args.photons, pe, 0, ws.data_ptr(), sp)
+        torch.cuda.synchronize()
+        ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush.zero_()
+        ea.record(stream)
+        tmc.photon_batch_device(tally.data_ptr(), args.photons, pe, 0, ws.data_ptr(), sp)
+        eb.record(stream)
+        torch.cuda.synchronize()
+        value_exact = args.photons * world / (ea.elapsed_time(eb) * 1e-3)
 
     # e2e through the host-array C ABI call
     e2e = None
@@ -345,6 +364,7 @@ def run_ours(args):
             "config": workload_config(args, world),
             "photon_steps_per_s": photon_steps_all / (total_ms * 1e-3),
             "steps_per_photon": photon_steps_all / photons_all,
+            "value_exact_math": value_exact,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu_base,
             "gpu_launches": args.steps, "clocks": clk, "wall_s_timed_region": t_wall,
         }
