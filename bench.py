@@ -56,6 +56,12 @@ def parse():
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", choices=["plain", "sweep"], default="plain",
+                    help="plain: config 1 (default); sweep: the 4096-problem batched sweep")
+    ap.add_argument("--sweep-scale", type=float, default=1.0 / 64,
+                    help="photon-count multiplier of the sweep (1 = full size, ~3.3e13 steps)")
+    ap.add_argument("--plain-steps", type=int, default=1,
+                    help="sweep workload: timed passes of the one-launch-per-problem form")
     return ap.parse_args()
 
 
@@ -374,10 +380,88 @@ def run_ours(args):
     return 0
 
 
+def run_sweep(args):
+    """Config 3: 4096 independent problems (seeded draw of the sweep's
+    parameter distribution) in one persistent launch per step, against the
+    plain form (one launch per problem, back to back on one stream)."""
+    import torch
+
+    import tiny_mc_gb300 as tmc
+    from tiny_mc_gb300.sweep import make_sweep
+
+    torch.cuda.set_device(0)
+    sw = make_sweep(4096, seed=0, photon_scale=args.sweep_scale, min_photons=16)
+    photons = int(sw["n_photons"].sum())
+    b = tmc.Batch(sw, seed=1, math=args.math)
+    t0 = time.perf_counter()
+    tune_ms = b.autotune(scale=min(1.0, 1.0 / 16), max_steps_per_photon=2e4)
+    tune_s = time.perf_counter() - t0
+    b.set_config(**{**b.config(), "use_graph": True})
+    _, est_steps = b.info()
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        b.run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(None)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        b.run(stream.cuda_stream)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = [a.elapsed_time(c) for a, c in ev]
+    _, steps_pp = b.read()
+    photon_steps = int(steps_pp.sum())     # one run's steps (each run zeroes the counters)
+    batched = photons * args.steps / (sum(ms) * 1e-3)
+
+    # the plain form: one tmc_photon_batch_device launch per problem
+    d = torch.zeros((int(sw["shells"].max()), 4), dtype=torch.int64, device="cuda")
+    ws = torch.zeros(max(1, tmc.workspace_bytes() // 8), dtype=torch.int64, device="cuda")
+    plist = [tmc.params(shells=int(q["shells"]), microns_per_shell=float(q["microns_per_shell"]),
+                        mu_a=float(q["mu_a"]), mu_s=float(q["mu_s"]), seed=1,
+                        photon_id_base=int(q["photon_id_base"]), math=args.math) for q in sw]
+    sp = stream.cuda_stream
+    plain_ms = []
+    for _ in range(max(1, args.plain_steps)):
+        a_, c_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a_.record(stream)
+        for q, p in zip(sw, plist):
+            tmc.photon_batch_device(d.data_ptr(), int(q["n_photons"]), p, 0, ws.data_ptr(), sp)
+        c_.record(stream)
+        torch.cuda.synchronize()
+        plain_ms.append(a_.elapsed_time(c_))
+    plain = photons * len(plain_ms) / (sum(plain_ms) * 1e-3)
+    n_items, _ = b.info()
+    line = {
+        "metric": METRIC, "value": batched, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sum(ms) / len(ms), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batched sweep (config 3): 4096 problems in one persistent launch",
+                   "photon_scale": args.sweep_scale, "photons_per_step": photons,
+                   "photon_steps_per_step": photon_steps,
+                   "est_photon_steps_per_step": est_steps, "math": args.math,
+                   "sweep_seed": 0, "rng_seed": 1, "batch_config": b.config(), "work_items": n_items,
+                   "autotune_s": tune_s, "autotune_best_ms": tune_ms},
+        "photon_steps_per_s": photon_steps * args.steps / (sum(ms) * 1e-3),
+        "plain_form": {"value": plain, "unit": UNIT, "ms_per_pass": sum(plain_ms) / len(plain_ms),
+                       "launches_per_pass": len(sw)},
+        "batched_over_plain": batched / plain,
+        "gpu_launches": args.steps, "clocks": clk,
+    }
+    b.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "sweep":
+        return run_sweep(args)
     return run_ours(args)
 
 

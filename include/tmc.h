@@ -147,6 +147,55 @@ int tmc_tally_to_heat(const tmc_tally *tally, const tmc_params *p, double *heat,
 int tmc_format_report(char *buf, size_t cap, const float *heat, const float *heat2,
                       uint64_t photons, const tmc_params *p);
 
+/* ------------------------------------------------------------------ batch
+ * Many independent walks in one persistent launch.  Each problem is what the
+ * reference computes for one set of params.h knobs (tiny_mc.c:34-69 run with
+ * one -D setting); the reference runs one problem per process.  All problems
+ * of a batch share one seed and arithmetic mode; give problems disjoint
+ * photon-id ranges for independent streams.  A problem's tally is
+ * bit-identical to tmc_photon_batch_fx on the same photons.
+ */
+typedef struct tmc_problem {
+    uint32_t shells;            /* SHELLS            */
+    float microns_per_shell;    /* MICRONS_PER_SHELL */
+    float mu_a;                 /* MU_A, 1/cm        */
+    float mu_s;                 /* MU_S, 1/cm        */
+    uint64_t n_photons;
+    uint64_t photon_id_base;
+} tmc_problem;
+
+typedef struct tmc_batch tmc_batch;   /* opaque plan with device buffers */
+
+typedef struct tmc_batch_config {
+    int block;            /* threads per block: 128, 256 or 512 (0 = 256) */
+    int items_per_block;  /* work items per resident block: load-balance granularity (0 = 8) */
+    int use_graph;        /* 1: run through a captured CUDA graph, replayed on later runs */
+} tmc_batch_config;
+
+int tmc_batch_create(tmc_batch **out, const tmc_problem *problems, uint32_t n_problems,
+                     uint64_t seed, uint32_t math);
+int tmc_batch_set_config(tmc_batch *b, const tmc_batch_config *cfg);
+int tmc_batch_get_config(const tmc_batch *b, tmc_batch_config *cfg);
+/* Times block size x items-per-block candidates on a reduced copy of the batch
+ * (photon counts x scale, problems above max_steps_per_photon expected steps
+ * left out; 0 = keep all) and keeps the fastest.  best_ms may be NULL. */
+int tmc_batch_autotune(tmc_batch *b, double scale, double max_steps_per_photon, double *best_ms);
+/* Zeroes the batch's device tallies and walks every problem (asynchronous on
+ * stream, a cudaStream_t or NULL). */
+int tmc_batch_run(tmc_batch *b, void *stream);
+/* Waits for the last run and copies tallies [total shells] (problem i's shells
+ * start at offsets[i]) and photon steps per problem; either may be NULL. */
+int tmc_batch_read(tmc_batch *b, tmc_tally *tallies, uint64_t *steps_per_problem);
+int tmc_batch_tally_offsets(const tmc_batch *b, uint64_t *offsets /* [n_problems + 1] */);
+int tmc_batch_info(const tmc_batch *b, uint32_t *n_items, double *est_photon_steps);
+/* Expected photon steps per photon for optics (mu_a, mu_s): photon.c's weight
+ * recursion (albedo^k, roulette at 0.001 with survival 0.1, photon.c:32,45-49)
+ * evaluated on the host.  The batch planner splits work with it. */
+int tmc_expected_steps(float mu_a, float mu_s, double *steps_per_photon);
+/* Device address of the batch's tallies (valid until destroy). */
+const void *tmc_batch_device_tallies(const tmc_batch *b);
+int tmc_batch_destroy(tmc_batch *b);
+
 /*
  * Launch shape of the plain walk: threads per block (128, 256 or 512; 0 =
  * default), resident blocks per SM (0 = occupancy limit) and a cap on the

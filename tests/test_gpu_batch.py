@@ -1,0 +1,113 @@
+"""The batched form on the GPU: every problem's tally in one persistent
+launch is bit-identical to the plain kernel's for the same photons, for any
+launch configuration, through CUDA-graph replay, and after autotuning."""
+import numpy as np
+import pytest
+
+from test_gpu_parity import as_array
+
+pytestmark = pytest.mark.gpu
+
+
+def small_sweep(n=40, seed=5, scale=1 / 512, max_albedo=0.999):
+    from tiny_mc_gb300.sweep import make_sweep
+    sw = make_sweep(4 * n, seed=seed, photon_scale=scale, min_photons=16)
+    albedo = sw["mu_s"] / (sw["mu_s"] + sw["mu_a"])
+    sw = sw[albedo < max_albedo][:n].copy()
+    # keep the ranges disjoint after the filter
+    sw["photon_id_base"] = np.concatenate([[0], np.cumsum(sw["n_photons"][:-1])])
+    return sw
+
+
+def plain_tally(tmc, prob, seed, math):
+    p = tmc.params(shells=int(prob["shells"]), microns_per_shell=float(prob["microns_per_shell"]),
+                   mu_a=float(prob["mu_a"]), mu_s=float(prob["mu_s"]), seed=seed,
+                   photon_id_base=int(prob["photon_id_base"]), math=math)
+    t, steps = tmc.photon_batch_fx(int(prob["n_photons"]), p)
+    return as_array(t), steps
+
+
+@pytest.mark.parametrize("math", ["exact", "fast"])
+def test_batch_equals_plain_per_problem(tmc_mod, math):
+    sw = small_sweep()
+    b = tmc_mod.Batch(sw, seed=7, math=math)
+    b.run()
+    tallies, steps = b.read()
+    for i in range(len(sw)):
+        ref, ref_steps = plain_tally(tmc_mod, sw[i], 7, math)
+        assert np.array_equal(as_array(b.tally_of(tallies, i)), ref), i
+        assert int(steps[i]) == ref_steps
+    b.close()
+
+
+def test_batch_equals_oracle(tmc_mod, oracle_mod):
+    sw = small_sweep(n=6, seed=11)
+    b = tmc_mod.Batch(sw, seed=3, math="exact")
+    b.run()
+    tallies, steps = b.read()
+    for i in range(len(sw)):
+        q = sw[i]
+        p = oracle_mod.oparams(int(q["shells"]), float(q["microns_per_shell"]), float(q["mu_a"]),
+                               float(q["mu_s"]), 3)
+        ref, _, ref_steps = oracle_mod.walk_fx(p, int(q["n_photons"]), id_base=int(q["photon_id_base"]))
+        assert np.array_equal(as_array(b.tally_of(tallies, i)), ref)
+        assert int(steps[i]) == ref_steps
+    b.close()
+
+
+@pytest.mark.parametrize("block,ipb,graph", [(128, 1, False), (256, 64, False), (512, 8, True),
+                                             (256, 8, True)])
+def test_batch_config_invariance(tmc_mod, block, ipb, graph):
+    sw = small_sweep(n=30, seed=8)
+    b = tmc_mod.Batch(sw, seed=2, math="fast")
+    b.run()
+    ref, ref_steps = b.read()
+    b.set_config(block, ipb, graph)
+    for _ in range(2):                 # second pass replays the graph
+        b.run()
+        t, s = b.read()
+        assert np.array_equal(t, ref) and np.array_equal(s, ref_steps)
+    assert b.config() == {"block": block, "items_per_block": ipb, "use_graph": graph}
+    b.close()
+
+
+def test_batch_autotune_keeps_results(tmc_mod):
+    sw = small_sweep(n=24, seed=9)
+    b = tmc_mod.Batch(sw, seed=4, math="fast")
+    b.run()
+    ref, _ = b.read()
+    ms = b.autotune(scale=0.25, max_steps_per_photon=2e4)
+    assert ms > 0
+    cfg = b.config()
+    assert cfg["block"] in (128, 256, 512) and cfg["items_per_block"] in (4, 8, 16)
+    b.run()
+    t, _ = b.read()
+    assert np.array_equal(t, ref)
+    b.close()
+
+
+def test_batch_edge_cases(tmc_mod):
+    from tiny_mc_gb300.sweep import PROBLEM_DTYPE
+    empty = np.zeros(0, PROBLEM_DTYPE)
+    b = tmc_mod.Batch(empty, seed=1)
+    b.run()
+    t, s = b.read()
+    assert t.size == 0 and s.size == 0
+    b.close()
+    two = np.zeros(2, PROBLEM_DTYPE)
+    two["shells"] = [5, 1]
+    two["microns_per_shell"] = 50
+    two["mu_a"] = [2.0, 1.0]
+    two["mu_s"] = [20.0, 0.0]
+    two["n_photons"] = [0, 100]
+    b = tmc_mod.Batch(two, seed=1)
+    b.run()
+    t, s = b.read()
+    assert not as_array(b.tally_of(t, 0)).any() and s[0] == 0
+    ref, ref_steps = plain_tally(tmc_mod, two[1], 1, "exact")
+    assert np.array_equal(as_array(b.tally_of(t, 1)), ref) and s[1] == ref_steps
+    b.close()
+    bad = two.copy()
+    bad["mu_a"][0] = 0.0
+    with pytest.raises(tmc_mod.TmcError):
+        tmc_mod.Batch(bad)

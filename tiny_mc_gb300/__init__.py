@@ -56,6 +56,12 @@ class Params(ctypes.Structure):
     ]
 
 
+class BatchConfig(ctypes.Structure):
+    """``tmc_batch_config``."""
+    _fields_ = [("block", ctypes.c_int), ("items_per_block", ctypes.c_int),
+                ("use_graph", ctypes.c_int)]
+
+
 TALLY_DTYPE = np.dtype([("w_lo", "<u8"), ("w_hi", "<u8"), ("w2_lo", "<u8"), ("w2_hi", "<u8")])
 
 _lib = None
@@ -88,6 +94,29 @@ def lib() -> ctypes.CDLL:
         L.tmc_set_plain_launch.restype = i32
         L.tmc_debug_rand.argtypes = [u64, u64, ctypes.c_uint32, vp]
         L.tmc_debug_rand.restype = i32
+        BP = ctypes.POINTER(ctypes.c_void_p)
+        L.tmc_batch_create.argtypes = [BP, vp, ctypes.c_uint32, u64, ctypes.c_uint32]
+        L.tmc_batch_create.restype = i32
+        L.tmc_batch_set_config.argtypes = [vp, ctypes.POINTER(BatchConfig)]
+        L.tmc_batch_set_config.restype = i32
+        L.tmc_batch_get_config.argtypes = [vp, ctypes.POINTER(BatchConfig)]
+        L.tmc_batch_get_config.restype = i32
+        L.tmc_batch_autotune.argtypes = [vp, ctypes.c_double, ctypes.c_double, vp]
+        L.tmc_batch_autotune.restype = i32
+        L.tmc_batch_run.argtypes = [vp, vp]
+        L.tmc_batch_run.restype = i32
+        L.tmc_batch_read.argtypes = [vp, vp, vp]
+        L.tmc_batch_read.restype = i32
+        L.tmc_batch_tally_offsets.argtypes = [vp, vp]
+        L.tmc_batch_tally_offsets.restype = i32
+        L.tmc_batch_info.argtypes = [vp, vp, vp]
+        L.tmc_batch_info.restype = i32
+        L.tmc_batch_device_tallies.argtypes = [vp]
+        L.tmc_batch_device_tallies.restype = vp
+        L.tmc_batch_destroy.argtypes = [vp]
+        L.tmc_batch_destroy.restype = i32
+        L.tmc_expected_steps.argtypes = [ctypes.c_float, ctypes.c_float, vp]
+        L.tmc_expected_steps.restype = i32
         L.tmc_photon_batch_static.argtypes = [vp, vp, u64, P, vp]
         L.tmc_photon_batch_static.restype = i32
         L.tmc_probe_sfu_rate.argtypes = [vp]
@@ -183,6 +212,79 @@ def workspace_bytes() -> int:
     return int(lib().tmc_workspace_bytes())
 
 
+def expected_steps(mu_a: float, mu_s: float) -> float:
+    """Expected photon steps per photon of photon.c's weight recursion (host)."""
+    out = ctypes.c_double(0.0)
+    _check(lib().tmc_expected_steps(mu_a, mu_s, ctypes.byref(out)), "tmc_expected_steps")
+    return out.value
+
+
+class Batch:
+    """Many independent problems in one persistent launch (``tmc_batch``).
+
+    ``problems`` is a structured array of ``sweep.PROBLEM_DTYPE``; all share
+    ``seed`` and the arithmetic mode."""
+
+    def __init__(self, problems: np.ndarray, seed: int = 1, math: str | int = "exact"):
+        from .sweep import PROBLEM_DTYPE
+        self.problems = np.ascontiguousarray(problems, dtype=PROBLEM_DTYPE)
+        m = {"exact": MATH_EXACT, "fast": MATH_FAST}.get(math, math) if isinstance(math, str) else math
+        h = ctypes.c_void_p()
+        _check(lib().tmc_batch_create(ctypes.byref(h), self.problems.ctypes.data, len(self.problems),
+                                      seed, int(m)), "tmc_batch_create")
+        self.handle = h
+        self.offsets = np.zeros(len(self.problems) + 1, np.uint64)
+        _check(lib().tmc_batch_tally_offsets(h, self.offsets.ctypes.data), "tmc_batch_tally_offsets")
+
+    def set_config(self, block: int = 0, items_per_block: int = 0, use_graph: bool = False) -> None:
+        c = BatchConfig(block, items_per_block, int(use_graph))
+        _check(lib().tmc_batch_set_config(self.handle, ctypes.byref(c)), "tmc_batch_set_config")
+
+    def config(self) -> dict:
+        c = BatchConfig()
+        _check(lib().tmc_batch_get_config(self.handle, ctypes.byref(c)), "tmc_batch_get_config")
+        return {"block": c.block, "items_per_block": c.items_per_block, "use_graph": bool(c.use_graph)}
+
+    def autotune(self, scale: float = 1.0 / 64, max_steps_per_photon: float = 2e4) -> float:
+        ms = ctypes.c_double(0.0)
+        _check(lib().tmc_batch_autotune(self.handle, scale, max_steps_per_photon, ctypes.byref(ms)),
+               "tmc_batch_autotune")
+        return ms.value
+
+    def run(self, stream: int = 0) -> None:
+        _check(lib().tmc_batch_run(self.handle, stream or None), "tmc_batch_run")
+
+    def read(self):
+        """(tallies [total shells] TALLY_DTYPE, photon steps per problem)."""
+        t = np.zeros(int(self.offsets[-1]), TALLY_DTYPE)
+        s = np.zeros(len(self.problems), np.uint64)
+        _check(lib().tmc_batch_read(self.handle, t.ctypes.data, s.ctypes.data), "tmc_batch_read")
+        return t, s
+
+    def info(self):
+        n = ctypes.c_uint32(0)
+        w = ctypes.c_double(0.0)
+        _check(lib().tmc_batch_info(self.handle, ctypes.byref(n), ctypes.byref(w)), "tmc_batch_info")
+        return n.value, w.value
+
+    def tally_of(self, tallies: np.ndarray, i: int) -> np.ndarray:
+        return tallies[int(self.offsets[i]):int(self.offsets[i + 1])]
+
+    def device_tallies(self) -> int:
+        return int(lib().tmc_batch_device_tallies(self.handle) or 0)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().tmc_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def tally_to_heat(tally: np.ndarray, p: Params):
     """FP64 heat, heat2 from exact tallies (host)."""
     heat = np.zeros(p.shells, np.float64)
@@ -221,6 +323,7 @@ def derived(p: Params):
 
 __all__ = [
     "Params", "params", "photon_batch", "photon_batch_fx", "photon_batch_device",
-    "workspace_bytes", "set_plain_launch", "debug_rand", "tally_to_heat", "tally_sums", "format_report", "derived", "TmcError",
+    "workspace_bytes", "set_plain_launch", "debug_rand", "tally_to_heat", "Batch", "BatchConfig",
+    "expected_steps", "photon_batch_static", "tally_sums", "format_report", "derived", "TmcError",
     "MATH_EXACT", "MATH_FAST", "TALLY_DTYPE", "lib", "LIB_PATH",
 ]

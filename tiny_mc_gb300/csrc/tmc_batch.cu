@@ -1,0 +1,630 @@
+// tmc_batch.cu — many independent walks (problems of different optics, shell
+// counts and photon counts) in ONE persistent launch.
+//
+// Reference: each problem is what tiny_mc.c:34-69 computes for one set of
+// params.h knobs; the reference runs one problem per process.  Here:
+//
+//  * the host splits every problem into work items (photon-id ranges) of
+//    roughly equal estimated photon steps — the expected steps per photon of
+//    photon.c's weight recursion times the photon count — so a problem of
+//    6e5 steps per photon is spread over many blocks while a problem of a few
+//    steps per photon stays one item; items are ordered heaviest first;
+//  * each resident block takes the next item from a global counter, zeroes
+//    its shared-memory histogram for that problem's shells, walks the item's
+//    photons with the same loop as the plain kernel (warps claim photons from
+//    a shared-memory counter), then adds the histogram to the problem's
+//    128-bit global tally and takes the next item;
+//  * results are integer tallies keyed by photon id, so each problem's tally
+//    is bit-identical to the plain kernel's for the same photons, whatever
+//    the item split, block size or order;
+//  * a batch can be replayed through a captured CUDA graph (zeroing + walk),
+//    and an autotuner picks block size and item granularity by timing a
+//    reduced copy of the batch.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "tmc_internal.h"
+#include "tmc_walk.cuh"
+
+namespace tmc {
+
+constexpr int BATCH_CHUNK = 32;   // photon ids a warp claims from its item at once
+
+struct BatchProblemDev {
+    WalkConsts c;
+    unsigned long long id_base;
+    unsigned long long tally_offset;   // in shells
+};
+
+struct BatchItemDev {
+    uint32_t problem;
+    uint32_t count;
+    unsigned long long first;          // first photon of the item, relative to the problem
+};
+
+struct BatchArgs {
+    PhiloxKeys keys;
+    const BatchProblemDev *problems;
+    const BatchItemDev *items;
+    uint32_t n_items;
+    uint32_t max_shells;
+    unsigned long long *tally;         // [total shells][4]
+    unsigned long long *steps;         // [problems]
+    unsigned long long *item_counter;  // zero at launch
+};
+
+template <int BLOCK, class M>
+__global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ uint32_t sh_item, sh_next;
+    uint32_t *my = smem + 4 * a.max_shells + threadIdx.x;
+
+    for (;;) {
+        if (threadIdx.x == 0) {
+            sh_item = (uint32_t)min(atomicAdd(a.item_counter, 1ull), 0xffffffffull);
+            sh_next = 0;
+        }
+        __syncthreads();
+        const uint32_t it = sh_item;
+        if (it >= a.n_items)
+            break;
+        const BatchItemDev item = a.items[it];
+        const BatchProblemDev pr = a.problems[item.problem];
+        const uint32_t S = pr.c.shells;
+        for (uint32_t s = threadIdx.x; s < 4 * S; s += BLOCK)
+            smem[s] = 0;
+        __syncthreads();
+
+        SharedSource<BATCH_CHUNK> src;
+        src.counter = &sh_next;
+        src.count = item.count;
+        src.first = pr.id_base + item.first;
+        unsigned long long *g = a.tally + 4 * pr.tally_offset;
+        const uint32_t steps = walk_loop<BLOCK, M>(pr.c, src, a.keys, smem, g, my);
+
+        __syncthreads();
+        flush_tally<BLOCK>(smem, S, g);
+        const unsigned long long tot = warp_sum_u64(steps);
+        if ((threadIdx.x & 31u) == 0 && tot)
+            atomicAdd(&a.steps[item.problem], tot);
+        __syncthreads();
+    }
+}
+
+namespace {
+
+// Expected photon steps per photon of photon.c's weight recursion: after k
+// steps the weight is albedo^k; the first time it drops below 0.001 the
+// photon survives with probability 0.1 and its weight is multiplied by 10.
+double expected_steps(float albedo)
+{
+    if (!(albedo > 0.0f))
+        return 1.0 / 0.9;
+    const double la = std::log((double)albedo);
+    double w = 1.0, e = 0.0, p = 1.0;
+    for (int stage = 0; stage < 12 && p > 1e-12; ++stage) {
+        double k = std::ceil(std::log(0.001 / w) / la);
+        if (k < 1.0)
+            k = 1.0;
+        e += p * k;
+        w = w * std::pow((double)albedo, k) / 0.1;
+        p *= 0.1;
+    }
+    return e;
+}
+
+}  // namespace
+
+}  // namespace tmc
+
+using namespace tmc;
+
+struct tmc_batch {
+    std::vector<tmc_problem> problems;
+    std::vector<Derived> derived;
+    std::vector<double> est_steps;
+    std::vector<unsigned long long> offsets;   // [n + 1] shell offsets
+    uint64_t seed = 0;
+    uint32_t math = TMC_MATH_EXACT;
+    uint32_t max_shells = 0;
+    tmc_batch_config cfg{256, 8, 0};
+    int device = -1;
+    int sms = 0;
+    int grid = 0;            // resident blocks for the current config (set by plan)
+    size_t smem_optin = 0;
+    // device buffers
+    BatchProblemDev *d_problems = nullptr;
+    BatchItemDev *d_items = nullptr;
+    uint32_t n_items = 0;
+    size_t items_cap = 0;
+    unsigned long long *d_tally = nullptr;
+    unsigned long long *d_steps = nullptr;
+    unsigned long long *d_counter = nullptr;
+    // graph
+    cudaGraphExec_t graph = nullptr;
+    cudaStream_t capture_stream = nullptr;
+    cudaStream_t last_stream = nullptr;
+    bool planned = false;
+};
+
+namespace {
+
+template <int BLOCK, class M>
+cudaError_t batch_kernel_config(int sms, size_t smem, int *grid)
+{
+    auto kern = walk_batch<BLOCK, M>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, smem);
+    if (e != cudaSuccess)
+        return e;
+    if (per_sm < 1)
+        return cudaErrorInvalidConfiguration;
+    *grid = sms * per_sm;
+    return cudaSuccess;
+}
+
+size_t batch_smem(const tmc_batch *b, int block)
+{
+    return (size_t)16 * b->max_shells + (size_t)4 * SLOTS * block;
+}
+
+cudaError_t grid_for(const tmc_batch *b, int *grid)
+{
+    const size_t smem = batch_smem(b, b->cfg.block);
+    const bool fast = b->math == TMC_MATH_FAST;
+    switch (b->cfg.block) {
+    case 128: return fast ? batch_kernel_config<128, FastMath>(b->sms, smem, grid)
+                          : batch_kernel_config<128, ExactMath>(b->sms, smem, grid);
+    case 256: return fast ? batch_kernel_config<256, FastMath>(b->sms, smem, grid)
+                          : batch_kernel_config<256, ExactMath>(b->sms, smem, grid);
+    case 512: return fast ? batch_kernel_config<512, FastMath>(b->sms, smem, grid)
+                          : batch_kernel_config<512, ExactMath>(b->sms, smem, grid);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+// Split problems into items of about equal estimated photon steps.
+int plan(tmc_batch *b)
+{
+    int grid = 0;
+    cudaError_t e = grid_for(b, &grid);   // also sets the kernel's shared-memory limit
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "batch kernel config");
+    b->grid = grid;
+    double total = 0.0;
+    for (size_t i = 0; i < b->problems.size(); ++i)
+        total += b->est_steps[i] * (double)b->problems[i].n_photons;
+    const double target = std::max(1.0, total / ((double)grid * std::max(1, b->cfg.items_per_block)));
+    const unsigned long long min_item = (unsigned long long)b->cfg.block * 2;
+    std::vector<std::pair<double, BatchItemDev>> items;
+    for (size_t i = 0; i < b->problems.size(); ++i) {
+        const unsigned long long n = b->problems[i].n_photons;
+        if (n == 0)
+            continue;
+        const double work = b->est_steps[i] * (double)n;
+        unsigned long long k = (unsigned long long)std::ceil(work / target);
+        k = std::max(1ull, std::min(k, (n + min_item - 1) / min_item));
+        k = std::max(k, (n + 0x3fffffffull) / 0x40000000ull);   // counts stay below 2^30
+        const unsigned long long per = n / k, extra = n % k;
+        unsigned long long at = 0;
+        for (unsigned long long j = 0; j < k; ++j) {
+            const unsigned long long c = per + (j < extra ? 1 : 0);
+            BatchItemDev it;
+            it.problem = (uint32_t)i;
+            it.count = (uint32_t)c;
+            it.first = at;
+            at += c;
+            items.push_back({b->est_steps[i] * (double)c, it});
+        }
+    }
+    std::stable_sort(items.begin(), items.end(),
+                     [](const auto &x, const auto &y) { return x.first > y.first; });
+    std::vector<BatchItemDev> h(items.size());
+    for (size_t i = 0; i < items.size(); ++i)
+        h[i] = items[i].second;
+    if (h.size() > b->items_cap) {
+        if (b->d_items)
+            cudaFree(b->d_items);
+        b->d_items = nullptr;
+        b->items_cap = 0;
+        e = cudaMalloc(&b->d_items, sizeof(BatchItemDev) * std::max<size_t>(1, h.size()));
+        if (e != cudaSuccess)
+            return set_cuda_error(e, "cudaMalloc(batch items)");
+        b->items_cap = std::max<size_t>(1, h.size());
+    }
+    if (!h.empty()) {
+        e = cudaMemcpy(b->d_items, h.data(), sizeof(BatchItemDev) * h.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess)
+            return set_cuda_error(e, "cudaMemcpy(batch items)");
+    }
+    b->n_items = (uint32_t)h.size();
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->planned = true;
+    return TMC_OK;
+}
+
+// Launch only (no attribute calls, so it can be captured): plan() has set
+// the kernel's shared-memory limit and the resident grid.
+template <int BLOCK, class M>
+cudaError_t launch_batch_t(const tmc_batch *b, cudaStream_t s)
+{
+    const size_t smem = batch_smem(b, BLOCK);
+    const int grid = std::max(1, std::min<int>(b->grid, (int)b->n_items));
+    BatchArgs a;
+    a.keys = make_philox_keys(b->seed);
+    a.problems = b->d_problems;
+    a.items = b->d_items;
+    a.n_items = b->n_items;
+    a.max_shells = b->max_shells;
+    a.tally = b->d_tally;
+    a.steps = b->d_steps;
+    a.item_counter = b->d_counter;
+    walk_batch<BLOCK, M><<<grid, BLOCK, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue(const tmc_batch *b, cudaStream_t s)
+{
+    const size_t n = b->problems.size();
+    cudaError_t e = cudaMemsetAsync(b->d_tally, 0, sizeof(tmc_tally) * b->offsets[n], s);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(b->d_steps, 0, sizeof(unsigned long long) * std::max<size_t>(1, n), s);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess || b->n_items == 0)
+        return e;
+    const bool fast = b->math == TMC_MATH_FAST;
+    switch (b->cfg.block) {
+    case 128: return fast ? launch_batch_t<128, FastMath>(b, s) : launch_batch_t<128, ExactMath>(b, s);
+    case 256: return fast ? launch_batch_t<256, FastMath>(b, s) : launch_batch_t<256, ExactMath>(b, s);
+    case 512: return fast ? launch_batch_t<512, FastMath>(b, s) : launch_batch_t<512, ExactMath>(b, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+int check_batch_device(const tmc_batch *b)
+{
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "cudaGetDevice");
+    if (dev != b->device) {
+        set_error_text("tmc_batch used on a different device than it was created on");
+        return TMC_E_STATE;
+    }
+    return TMC_OK;
+}
+
+void free_batch(tmc_batch *b)
+{
+    if (!b)
+        return;
+    if (b->graph)
+        cudaGraphExecDestroy(b->graph);
+    if (b->capture_stream)
+        cudaStreamDestroy(b->capture_stream);
+    cudaFree(b->d_problems);
+    cudaFree(b->d_items);
+    cudaFree(b->d_tally);
+    cudaFree(b->d_steps);
+    cudaFree(b->d_counter);
+    delete b;
+}
+
+int run_locked(tmc_batch *b, void *stream)
+{
+    int st = check_batch_device(b);
+    if (st)
+        return st;
+    if (!b->planned && (st = plan(b)))
+        return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaError_t e;
+    if (b->cfg.use_graph) {
+        if (!b->graph) {
+            if (!b->capture_stream &&
+                (e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking)) != cudaSuccess)
+                return set_cuda_error(e, "cudaStreamCreate(capture)");
+            cudaGraph_t g = nullptr;
+            e = cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess)
+                return set_cuda_error(e, "cudaStreamBeginCapture");
+            cudaError_t e1 = enqueue(b, b->capture_stream);
+            e = cudaStreamEndCapture(b->capture_stream, &g);
+            if (e1 != cudaSuccess || e != cudaSuccess) {
+                if (g)
+                    cudaGraphDestroy(g);
+                return set_cuda_error(e1 != cudaSuccess ? e1 : e, "batch graph capture");
+            }
+            e = cudaGraphInstantiate(&b->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                b->graph = nullptr;
+                return set_cuda_error(e, "cudaGraphInstantiate");
+            }
+        }
+        e = cudaGraphLaunch(b->graph, s);
+    } else {
+        e = enqueue(b, s);
+    }
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "tmc_batch_run");
+    b->last_stream = s;
+    return TMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tmc_batch_create(tmc_batch **out, const tmc_problem *problems, uint32_t n_problems, uint64_t seed,
+                     uint32_t math)
+{
+    if (!out || (n_problems && !problems))
+        return TMC_E_INVALID;
+    if (math != TMC_MATH_EXACT && math != TMC_MATH_FAST)
+        return TMC_E_INVALID;
+    *out = nullptr;
+    unsigned long long total_shells = 0;
+    uint32_t max_shells = 1;
+    for (uint32_t i = 0; i < n_problems; ++i) {
+        tmc_params p;
+        tmc_params_default(&p);
+        p.shells = problems[i].shells;
+        p.microns_per_shell = problems[i].microns_per_shell;
+        p.mu_a = problems[i].mu_a;
+        p.mu_s = problems[i].mu_s;
+        p.math = math;
+        int st = validate(&p);
+        if (st)
+            return st;
+        if (problems[i].n_photons > (1ull << 62) ||
+            problems[i].photon_id_base > ~0ull - problems[i].n_photons)
+            return TMC_E_OVERFLOW;
+        total_shells += problems[i].shells;
+        max_shells = std::max(max_shells, problems[i].shells);
+    }
+    std::lock_guard<std::mutex> lk(api_mutex());
+    int st = TMC_OK;
+    DeviceCtx *c = current_ctx(&st);
+    if (!c)
+        return st;
+    std::unique_ptr<tmc_batch> b(new tmc_batch);
+    b->problems.assign(problems, problems + n_problems);
+    b->seed = seed;
+    b->math = math;
+    b->max_shells = max_shells;
+    b->device = c->device;
+    b->sms = c->sms;
+    b->smem_optin = c->smem_optin;
+    if (batch_smem(b.get(), 512) > b->smem_optin) {
+        b->cfg.block = 256;
+        if (batch_smem(b.get(), 256) > b->smem_optin) {
+            set_error_text("tmc_batch_create: too many shells for the shared-memory histogram");
+            return TMC_E_INVALID;
+        }
+    }
+    b->offsets.resize(n_problems + 1);
+    std::vector<BatchProblemDev> hp(n_problems);
+    b->offsets[0] = 0;
+    for (uint32_t i = 0; i < n_problems; ++i) {
+        const tmc_problem &q = problems[i];
+        const Derived d = derive(q.mu_a, q.mu_s, q.microns_per_shell, q.shells);
+        b->derived.push_back(d);
+        b->est_steps.push_back(expected_steps(d.albedo));
+        hp[i].c.albedo = d.albedo;
+        hp[i].c.spm = d.spm;
+        hp[i].c.last = d.last;
+        hp[i].c.shells = d.shells;
+        hp[i].id_base = q.photon_id_base;
+        hp[i].tally_offset = b->offsets[i];
+        b->offsets[i + 1] = b->offsets[i] + q.shells;
+    }
+    cudaError_t e = cudaMalloc(&b->d_problems, sizeof(BatchProblemDev) * std::max<size_t>(1, n_problems));
+    if (e == cudaSuccess && n_problems)
+        e = cudaMemcpy(b->d_problems, hp.data(), sizeof(BatchProblemDev) * n_problems, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&b->d_tally, sizeof(tmc_tally) * std::max<unsigned long long>(1, total_shells));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&b->d_steps, sizeof(unsigned long long) * std::max<size_t>(1, n_problems));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&b->d_counter, sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        int r = set_cuda_error(e, "tmc_batch_create");
+        free_batch(b.release());
+        return r;
+    }
+    *out = b.release();
+    return TMC_OK;
+}
+
+int tmc_batch_set_config(tmc_batch *b, const tmc_batch_config *cfg)
+{
+    if (!b || !cfg)
+        return TMC_E_INVALID;
+    const int block = cfg->block ? cfg->block : 256;
+    if (block != 128 && block != 256 && block != 512)
+        return TMC_E_INVALID;
+    if (cfg->items_per_block < 0 || cfg->items_per_block > 1024)
+        return TMC_E_INVALID;
+    if (batch_smem(b, block) > b->smem_optin)
+        return TMC_E_INVALID;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    const bool replan = block != b->cfg.block || (cfg->items_per_block ? cfg->items_per_block : 8) !=
+                                                    b->cfg.items_per_block;
+    b->cfg.block = block;
+    b->cfg.items_per_block = cfg->items_per_block ? cfg->items_per_block : 8;
+    if (b->cfg.use_graph != (cfg->use_graph ? 1 : 0) && b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->cfg.use_graph = cfg->use_graph ? 1 : 0;
+    if (replan)
+        b->planned = false;
+    return TMC_OK;
+}
+
+int tmc_batch_get_config(const tmc_batch *b, tmc_batch_config *cfg)
+{
+    if (!b || !cfg)
+        return TMC_E_INVALID;
+    *cfg = b->cfg;
+    return TMC_OK;
+}
+
+int tmc_batch_run(tmc_batch *b, void *stream)
+{
+    if (!b)
+        return TMC_E_INVALID;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    return run_locked(b, stream);
+}
+
+int tmc_batch_read(tmc_batch *b, tmc_tally *tallies, uint64_t *steps_per_problem)
+{
+    if (!b)
+        return TMC_E_INVALID;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    int st = check_batch_device(b);
+    if (st)
+        return st;
+    cudaError_t e = cudaStreamSynchronize(b->last_stream);
+    const size_t n = b->problems.size();
+    if (e == cudaSuccess && tallies)
+        e = cudaMemcpy(tallies, b->d_tally, sizeof(tmc_tally) * b->offsets[n], cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && steps_per_problem && n)
+        e = cudaMemcpy(steps_per_problem, b->d_steps, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "tmc_batch_read");
+    return TMC_OK;
+}
+
+int tmc_batch_tally_offsets(const tmc_batch *b, uint64_t *offsets)
+{
+    if (!b || !offsets)
+        return TMC_E_INVALID;
+    for (size_t i = 0; i < b->offsets.size(); ++i)
+        offsets[i] = b->offsets[i];
+    return TMC_OK;
+}
+
+int tmc_batch_info(const tmc_batch *b, uint32_t *n_items, double *est_photon_steps)
+{
+    if (!b)
+        return TMC_E_INVALID;
+    if (n_items)
+        *n_items = b->n_items;
+    if (est_photon_steps) {
+        double t = 0.0;
+        for (size_t i = 0; i < b->problems.size(); ++i)
+            t += b->est_steps[i] * (double)b->problems[i].n_photons;
+        *est_photon_steps = t;
+    }
+    return TMC_OK;
+}
+
+const void *tmc_batch_device_tallies(const tmc_batch *b) { return b ? b->d_tally : nullptr; }
+
+int tmc_expected_steps(float mu_a, float mu_s, double *steps_per_photon)
+{
+    if (!steps_per_photon)
+        return TMC_E_INVALID;
+    tmc_params p;
+    tmc_params_default(&p);
+    p.mu_a = mu_a;
+    p.mu_s = mu_s;
+    int st = validate(&p);
+    if (st)
+        return st;
+    *steps_per_photon = expected_steps(derive(mu_a, mu_s, 50.0f, 1).albedo);
+    return TMC_OK;
+}
+
+int tmc_batch_autotune(tmc_batch *b, double scale, double max_steps_per_photon, double *best_ms)
+{
+    if (!b || !(scale > 0.0) || scale > 1.0)
+        return TMC_E_INVALID;
+    // a reduced copy: photon counts scaled, problems with very long walks left
+    // out (a single photon of those would dominate every timing)
+    std::vector<tmc_problem> red;
+    for (size_t i = 0; i < b->problems.size(); ++i) {
+        if (max_steps_per_photon > 0.0 && b->est_steps[i] > max_steps_per_photon)
+            continue;
+        tmc_problem q = b->problems[i];
+        q.n_photons = std::max<uint64_t>(64, (uint64_t)std::ceil((double)q.n_photons * scale));
+        red.push_back(q);
+    }
+    if (red.empty())
+        return TMC_OK;
+    tmc_batch *t = nullptr;
+    int st = tmc_batch_create(&t, red.data(), (uint32_t)red.size(), b->seed, b->math);
+    if (st)
+        return st;
+    static const int blocks[3] = {128, 256, 512};
+    static const int ipb[3] = {4, 8, 16};
+    double best = 1e300;
+    tmc_batch_config best_cfg = b->cfg;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e1);
+    for (int bi = 0; bi < 3 && e == cudaSuccess && st == TMC_OK; ++bi) {
+        for (int ii = 0; ii < 3 && e == cudaSuccess && st == TMC_OK; ++ii) {
+            tmc_batch_config c{blocks[bi], ipb[ii], 0};
+            if (tmc_batch_set_config(t, &c) != TMC_OK)
+                continue;
+            st = tmc_batch_run(t, nullptr);          // warm-up and planning
+            if (st)
+                break;
+            e = cudaEventRecord(e0, nullptr);
+            if (e == cudaSuccess)
+                st = tmc_batch_run(t, nullptr);
+            if (e == cudaSuccess)
+                e = cudaEventRecord(e1, nullptr);
+            if (e == cudaSuccess)
+                e = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (e == cudaSuccess)
+                e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e == cudaSuccess && st == TMC_OK && ms < best) {
+                best = ms;
+                best_cfg = c;
+            }
+        }
+    }
+    if (e0)
+        cudaEventDestroy(e0);
+    if (e1)
+        cudaEventDestroy(e1);
+    free_batch(t);
+    if (st)
+        return st;
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "tmc_batch_autotune");
+    best_cfg.use_graph = b->cfg.use_graph;
+    st = tmc_batch_set_config(b, &best_cfg);
+    if (best_ms)
+        *best_ms = best;
+    return st;
+}
+
+int tmc_batch_destroy(tmc_batch *b)
+{
+    if (!b)
+        return TMC_OK;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    free_batch(b);
+    return TMC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,284 @@
+// tmc_walk.cuh — the photon-walk loop shared by the plain and batched kernels.
+//
+// Reference path: tiny_mc.c:47-49 calls photon() (photon.c:6-51) once per
+// photon.  Here every thread of a persistent grid carries one photon at a
+// time and warps refill dead lanes with new photon ids:
+//
+//  * when a photon dies in the roulette (photon.c:45-49) its lane takes the
+//    next photon id from a chunk its warp claimed from a PhotonSource (a
+//    global counter for the plain kernel, a shared-memory counter over one
+//    work item for the batched kernel), so lanes never idle while work
+//    remains;
+//  * the rejection loop of photon.c:36-40 is folded into the main loop: each
+//    iteration evaluates the next two rejection tries from the buffered
+//    stream and consumes only the words photon.c would (two if the first try
+//    is accepted, four otherwise).  A photon whose two tries both failed
+//    (p = 0.046) skips the move/absorb part on the next iteration, so lanes
+//    of a warp stay in lock-step instead of waiting for the lane with the
+//    most retries;
+//  * random words come from a per-thread ring of 16 words in shared memory,
+//    refilled four at a time from Philox; slots 16..21 mirror 0..5 so the
+//    <= 6 words one iteration reads are fixed offsets from one base.  The
+//    refill at the top keeps >= 6 words buffered (an iteration consumes at
+//    most six: step, four for two tries, roulette), runs only when some lane
+//    is short, and then every lane with room refills, so Philox runs with
+//    most lanes active;
+//  * the two tallies of photon.c:30-31 go into a per-block shared-memory
+//    histogram of 64-bit fixed-point sums (sum of w and of w^2, 2^-40 units),
+//    each kept as two 32-bit words updated with native 32-bit shared atomics
+//    (a 64-bit shared atomicAdd is a compare-and-swap loop); a wrap of a
+//    64-bit shared sum carries 2^64 into the 128-bit global tally.
+#pragma once
+
+#include "tmc_device.cuh"
+
+namespace tmc {
+
+constexpr int RING = 16;        // random words buffered per thread
+constexpr int MIRROR = 6;       // slots 16..21 repeat slots 0..5
+constexpr int SLOTS = RING + MIRROR;
+
+// Per-problem constants of photon.c:8-9 (computed on the host in float,
+// exactly as photon.c does) plus the shell count.
+struct WalkConsts {
+    float albedo;
+    float spm;     // shells_per_mfp
+    float last;    // (float)(shells - 1)
+    uint32_t shells;
+};
+
+// Photon ids from a global 64-bit counter over [0, n): each warp claims
+// CHUNK ids per atomic.
+template <int CHUNK>
+struct GlobalSource {
+    unsigned long long *counter;
+    unsigned long long n;
+    unsigned long long id_base;
+    unsigned long long cnext = 0, cend = 0;
+    bool exhausted = false;
+
+    // Warp-collective.  need = ballot of lanes wanting a photon, rank = this
+    // lane's index among them.  Returns true and the photon id if this lane
+    // got one (only meaningful for wanting lanes).
+    __device__ __forceinline__ bool next(unsigned need, unsigned rank, unsigned lane,
+                                         unsigned long long &pid)
+    {
+        const unsigned n_need = __popc(need);
+        unsigned long long id = cnext + rank;
+        bool got = rank < cend - cnext;
+        if (n_need > cend - cnext) {
+            const unsigned take0 = (unsigned)(cend - cnext);
+            unsigned long long base = 0;
+            if (!exhausted) {
+                if (lane == 0)
+                    base = atomicAdd(counter, (unsigned long long)CHUNK);
+                base = __shfl_sync(FULL_MASK, base, 0);
+                exhausted = base >= n;
+            }
+            if (exhausted) {
+                cnext = cend;
+            } else {
+                cend = min(base + (unsigned long long)CHUNK, n);
+                if (!got) {
+                    id = base + (rank - take0);
+                    got = id < cend;
+                }
+                cnext = min(base + (n_need - take0), cend);
+            }
+        } else {
+            cnext += n_need;
+        }
+        pid = id_base + id;
+        return got;
+    }
+};
+
+// Photon ids from a shared-memory 32-bit counter over one work item of
+// `count` photons starting at id `first`.
+template <int CHUNK>
+struct SharedSource {
+    uint32_t *counter;   // shared memory, zero at the start of the item
+    uint32_t count;
+    unsigned long long first;
+    uint32_t cnext = 0, cend = 0;
+    bool exhausted = false;
+
+    __device__ __forceinline__ bool next(unsigned need, unsigned rank, unsigned lane,
+                                         unsigned long long &pid)
+    {
+        const unsigned n_need = __popc(need);
+        uint32_t id = cnext + rank;
+        bool got = rank < cend - cnext;
+        if (n_need > cend - cnext) {
+            const unsigned take0 = cend - cnext;
+            uint32_t base = 0;
+            if (!exhausted) {
+                if (lane == 0)
+                    base = atomicAdd(counter, (uint32_t)CHUNK);
+                base = __shfl_sync(FULL_MASK, base, 0);
+                exhausted = base >= count;
+            }
+            if (exhausted) {
+                cnext = cend;
+            } else {
+                cend = min(base + (uint32_t)CHUNK, count);
+                if (!got) {
+                    id = base + (rank - take0);
+                    got = id < cend;
+                }
+                cnext = min(base + (n_need - take0), cend);
+            }
+        } else {
+            cnext += n_need;
+        }
+        pid = first + id;
+        return got;
+    }
+};
+
+// Walk photons from `src` until it is exhausted and every lane's photon has
+// died.  Warp-collective: all 32 lanes of every warp call it.  tally: the
+// block's shared histogram, 4 * shells words (low and high of sum w, then of
+// sum w^2); g: the problem's global 128-bit tally [shells][4] (receives only
+// carries here).  Returns this thread's photon steps.
+template <int BLOCK, class M, class Source>
+__device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
+                                              const PhiloxKeys &keys, uint32_t *tally,
+                                              unsigned long long *g, uint32_t *my)
+{
+    const uint32_t S = c.shells;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt_mask = (1u << lane) - 1u;
+
+    bool alive = false, want = true, pending = false;
+    uint32_t pid_lo = 0, pid_hi = 0, blk = 0, prod = 0, cur = 0;
+    float x = 0.f, y = 0.f, z = 0.f, u = 0.f, v = 0.f, w = 1.f, weight = 1.f;
+    uint32_t steps = 0;
+
+    for (;;) {
+        // -------- hand new photon ids to lanes whose photon died
+        const unsigned need = __ballot_sync(FULL_MASK, want);
+        if (need) {
+            unsigned long long pid = 0;
+            const bool got = src.next(need, __popc(need & lt_mask), lane, pid);
+            if (want) {
+                want = false;
+                alive = got;
+                // launch, photon.c:12-18
+                pid_lo = (uint32_t)pid;
+                pid_hi = (uint32_t)(pid >> 32);
+                blk = 0;
+                cur = prod;   // drop words buffered for the previous photon
+                pending = false;
+                x = y = z = 0.f;
+                u = v = 0.f;
+                w = 1.f;
+                weight = 1.f;
+            }
+            // lanes change from alive to idle only here
+            if (__ballot_sync(FULL_MASK, alive) == 0)
+                break;
+        }
+
+        // -------- keep >= 6 random words buffered (one iteration uses <= 6);
+        // a fresh photon starts empty and needs two passes
+        while (__any_sync(FULL_MASK, alive && (prod - cur) < 6u)) {
+            if (alive && (prod - cur) <= (uint32_t)(RING - 4)) {
+                const uint4 r = philox4x32_10(blk, 0u, pid_lo, pid_hi, keys);
+                ++blk;
+                const uint32_t p = prod & (RING - 1);
+                uint32_t *dst = my + p * BLOCK;
+                dst[0 * BLOCK] = r.x;
+                dst[1 * BLOCK] = r.y;
+                dst[2 * BLOCK] = r.z;
+                dst[3 * BLOCK] = r.w;
+                // mirror: slots 16..19 repeat 0..3, slots 20..21 repeat 4..5
+                uint32_t *mir = dst + RING * BLOCK;
+                if (p <= 4u) {
+                    mir[0 * BLOCK] = r.x;
+                    mir[1 * BLOCK] = r.y;
+                }
+                if (p == 0u) {
+                    mir[2 * BLOCK] = r.z;
+                    mir[3 * BLOCK] = r.w;
+                }
+                prod += 4;
+            }
+        }
+
+        if (alive) {
+            // the <= 6 words this iteration may read, from one base
+            const uint32_t *rd = my + (cur & (RING - 1)) * BLOCK;
+            if (!pending) {
+                // move, photon.c:21-24
+                const float U = uniform01(rd[0]);
+                rd += BLOCK;
+                ++cur;
+                const float t = M::step_length(U);
+                x = M::move(x, t, u);
+                y = M::move(y, t, v);
+                z = M::move(z, t, w);
+                // absorb, photon.c:26-32 (clamp in float: same shell for every
+                // radius below 2^32 shells, and a NaN radius lands last)
+                const float rr = M::radius_shells(x, y, z, c.spm);
+                const uint32_t shell = __float2uint_rz(fminf(rr, c.last));
+                uint32_t *t0 = tally + shell;
+                uint32_t lo, hi;
+                fx40_split(weight, lo, hi);
+                tally_add(t0, t0 + S, &g[4 * shell + 1], lo, hi);
+                fx40_split(__fmul_rn(weight, weight), lo, hi);
+                tally_add(t0 + 2 * S, t0 + 3 * S, &g[4 * shell + 3], lo, hi);
+                weight = M::mul(weight, c.albedo);
+                ++steps;
+            }
+            // the next two tries of the rejection method, photon.c:36-40; the
+            // second one's words are consumed only if the first is rejected
+            const float xa1 = uniform_pm1(rd[0 * BLOCK]);
+            const float xa2 = uniform_pm1(rd[1 * BLOCK]);
+            const float xb1 = uniform_pm1(rd[2 * BLOCK]);
+            const float xb2 = uniform_pm1(rd[3 * BLOCK]);
+            const float ta = M::norm2(xa1, xa2);
+            const float tb = M::norm2(xb1, xb2);
+            const bool first = !(1.0f < ta);
+            const float xi1 = first ? xa1 : xb1;
+            const float xi2 = first ? xa2 : xb2;
+            const float tt = first ? ta : tb;
+            rd += first ? 2 * BLOCK : 4 * BLOCK;
+            cur += first ? 2u : 4u;
+            pending = (1.0f < tt);
+            if (!pending) {
+                // new direction, photon.c:41-43
+                u = fmaf(2.0f, tt, -1.0f);
+                const float sc = M::dir_scale(tt, u);
+                v = M::mul(xi1, sc);
+                w = M::mul(xi2, sc);
+                // roulette, photon.c:45-49
+                if (weight < 0.001f) {
+                    const float U = uniform01(rd[0]);
+                    ++cur;
+                    if (U > 0.1f) {
+                        alive = false;
+                        want = true;
+                    } else {
+                        weight = __fdiv_rn(weight, 0.1f);
+                    }
+                }
+            }
+        }
+    }
+    return steps;
+}
+
+// Add a block's shared histogram (4 * shells words) into a 128-bit global
+// tally [shells][4].  Block-collective, after a barrier.
+template <int BLOCK>
+__device__ __forceinline__ void flush_tally(const uint32_t *tally, uint32_t S, unsigned long long *g)
+{
+    for (uint32_t s = threadIdx.x; s < S; s += BLOCK) {
+        flush128(&g[4 * s + 0], &g[4 * s + 1], ((unsigned long long)tally[S + s] << 32) | tally[s]);
+        flush128(&g[4 * s + 2], &g[4 * s + 3],
+                 ((unsigned long long)tally[3 * S + s] << 32) | tally[2 * S + s]);
+    }
+}
+
+}  // namespace tmc
