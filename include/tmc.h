@@ -196,6 +196,71 @@ int tmc_expected_steps(float mu_a, float mu_s, double *steps_per_photon);
 const void *tmc_batch_device_tallies(const tmc_batch *b);
 int tmc_batch_destroy(tmc_batch *b);
 
+/* ----------------------------------------------------------------- server
+ * Continuous batching of simulation requests, each stopped at a target
+ * relative standard error.  No counterpart in the reference (one run per
+ * process); each request is one tiny_mc.c run with its own knobs.  A request
+ * is walked in RSE batches; at fixed batch counts (min_batches, then
+ * doubling) the batch-means RSE of the heat in `probe_shell` is computed in
+ * FP64 and the request stops when it is <= target_rse or max_photons is
+ * reached.  Results depend only on the request (optics, photon_id_base,
+ * server seed and arithmetic), not on what else runs.
+ */
+typedef struct tmc_request {
+    uint32_t shells;
+    float microns_per_shell;
+    float mu_a;
+    float mu_s;
+    double target_rse;          /* e.g. 0.01 for 1 % */
+    uint64_t max_photons;       /* cap */
+    uint64_t photon_id_base;    /* first photon id of this request's streams */
+} tmc_request;
+
+typedef struct tmc_request_result {
+    uint64_t photons;           /* photons walked (batches x batch_photons) */
+    uint64_t photon_steps;
+    uint32_t batches;
+    uint32_t batch_photons;
+    double rse;                 /* batch-means RSE at the stop (NaN if the shell got nothing) */
+    int32_t reached_target;     /* 1: rse <= target; 0: stopped at the cap */
+    int32_t reserved;
+    double latency_s;           /* completion - submission (run_trace: - arrival) */
+} tmc_request_result;
+
+typedef struct tmc_server_config {
+    uint32_t slots;                 /* requests resident at once (tally memory) */
+    uint32_t max_shells;            /* tally memory per slot: max_shells x 32 bytes */
+    uint32_t probe_shell;           /* shell of the RSE (10 = 500-550 um at 50 um shells) */
+    uint32_t min_batches;           /* first stop decision */
+    uint64_t seed;
+    uint32_t math;
+    uint32_t block;                 /* 128, 256 or 512 */
+    uint32_t max_items_per_request; /* RSE batches of one request in one wave */
+    uint32_t reserved;
+    double steps_per_batch;         /* target photon steps per RSE batch */
+} tmc_server_config;
+
+typedef struct tmc_server tmc_server;
+
+void tmc_server_config_default(tmc_server_config *c);
+int tmc_server_create(tmc_server **out, const tmc_server_config *cfg);
+/* TMC_E_BUSY when no slot is free (the caller queues the request). */
+int tmc_server_submit(tmc_server *s, const tmc_request *r, uint64_t *request_id);
+/* Non-blocking: harvests finished waves, makes stop decisions, launches the
+ * next wave on a free stream. */
+int tmc_server_progress(tmc_server *s, uint32_t *waves_in_flight, uint32_t *active_requests);
+int tmc_server_poll(tmc_server *s, uint64_t request_id, int *done);
+/* Result of a finished request (then forgotten); tally [shells] may be NULL. */
+int tmc_server_result(tmc_server *s, uint64_t request_id, tmc_tally *tally, tmc_request_result *res);
+int tmc_server_stats(tmc_server *s, uint64_t *photons, uint64_t *photon_steps, uint64_t *waves);
+/* Replays an arrival trace in real time (arrival_s sorted, seconds from the
+ * start): admits requests as they arrive and slots free up, drives the server
+ * until all complete or time_limit_s (0 = none) passes.  results[i] is zero
+ * for requests not completed; latency is completion - arrival. */
+int tmc_server_run_trace(tmc_server *s, const tmc_request *reqs, const double *arrival_s, uint32_t n,
+                         double time_limit_s, tmc_request_result *results, uint32_t *completed);
+int tmc_server_destroy(tmc_server *s);
+
 /*
  * Launch shape of the plain walk: threads per block (128, 256 or 512; 0 =
  * default), resident blocks per SM (0 = occupancy limit) and a cap on the

@@ -1,0 +1,96 @@
+"""The request server on the GPU: a request's result is the same alone and in
+a mix of concurrent requests, equals the plain kernel over the same photons,
+stops by its rule, and admission refuses requests when slots are full."""
+import numpy as np
+import pytest
+
+from test_gpu_parity import as_array
+
+pytestmark = pytest.mark.gpu
+
+
+def req(mu_a=2.0, mu_s=20.0, shells=101, rse=0.02, cap=1 << 20, base=0):
+    from tiny_mc_gb300.serve import REQUEST_DTYPE
+    r = np.zeros(1, REQUEST_DTYPE)[0]
+    r["shells"], r["microns_per_shell"], r["mu_a"], r["mu_s"] = shells, 50.0, mu_a, mu_s
+    r["target_rse"], r["max_photons"], r["photon_id_base"] = rse, cap, base
+    return r
+
+
+MIX = [req(2.0, 20.0, 101, 0.02, base=1 << 32), req(0.5, 50.0, 501, 0.03, base=2 << 32),
+       req(5.0, 5.0, 101, 0.01, base=3 << 32), req(1.0, 300.0, 501, 0.05, base=4 << 32),
+       req(0.02, 2.0, 101, 0.04, cap=1 << 16, base=5 << 32)]
+
+
+def test_alone_equals_in_mix(tmc_mod):
+    from tiny_mc_gb300.serve import Server
+    probe = req(1.0, 30.0, 101, 0.02, base=9 << 32)
+    s = Server(slots=8)
+    rid = s.submit(probe)
+    alone = s.run({rid: 101})[rid]
+    s.close()
+    s = Server(slots=8)
+    ids = {s.submit(r): int(r["shells"]) for r in MIX[:3]}
+    rid = s.submit(probe)
+    ids[rid] = 101
+    ids.update({s.submit(r): int(r["shells"]) for r in MIX[3:]})
+    out = s.run(ids)
+    s.close()
+    t_alone, r_alone = alone
+    t_mix, r_mix = out[rid]
+    assert np.array_equal(t_alone, t_mix)
+    for f in ("photons", "photon_steps", "batches", "batch_photons", "reached_target"):
+        assert r_alone[f] == r_mix[f], f
+    assert r_alone["rse"] == r_mix["rse"]
+
+
+def test_result_equals_plain_kernel_and_rule(tmc_mod):
+    from tiny_mc_gb300.serve import Server
+    s = Server(slots=8)
+    ids = {s.submit(r): int(r["shells"]) for r in MIX}
+    out = s.run(ids)
+    s.close()
+    for (rid, sh), r in zip(ids.items(), MIX):
+        tally, res = out[rid]
+        n = int(res["photons"])
+        assert n == int(res["batches"]) * int(res["batch_photons"])
+        p = tmc_mod.params(shells=sh, microns_per_shell=50.0, mu_a=float(r["mu_a"]), mu_s=float(r["mu_s"]),
+                           seed=1, photon_id_base=int(r["photon_id_base"]), math="fast")
+        ref, steps = tmc_mod.photon_batch_fx(n, p)
+        assert np.array_equal(as_array(tally), as_array(ref))
+        assert int(res["photon_steps"]) == steps
+        b = int(res["batches"])
+        if res["reached_target"]:
+            assert res["rse"] <= r["target_rse"]
+        else:
+            assert n >= int(r["max_photons"]) or b * int(res["batch_photons"]) >= int(r["max_photons"])
+        # decisions only at 32, 64, 128, ... batches, or at the cap
+        cap_b = -(-int(r["max_photons"]) // int(res["batch_photons"]))
+        assert b == cap_b or (b >= 32 and (b & (b - 1)) == 0)
+
+
+def test_admission_refuses_when_full(tmc_mod):
+    from tiny_mc_gb300.serve import Server
+    s = Server(slots=2)
+    a = s.submit(MIX[0])
+    b = s.submit(MIX[1])
+    assert a is not None and b is not None
+    assert s.submit(MIX[2]) is None          # TMC_E_BUSY: the caller queues
+    s.run({a: 101, b: 501})
+    c = s.submit(MIX[2])                      # a slot freed up
+    assert c is not None
+    s.run({c: 101})
+    s.close()
+
+
+def test_run_trace_small(tmc_mod):
+    from tiny_mc_gb300.serve import Server, make_trace
+    req_, arr = make_trace(60, rate=400.0, seed=3, mu_a_range=(0.5, 10.0), mu_s_range=(1.0, 100.0),
+                           rse=(0.02, 0.05), max_photons=1 << 18)
+    s = Server(slots=16)
+    res, done = s.run_trace(req_, arr, time_limit_s=120.0)
+    assert done == 60
+    assert np.all(res["latency_s"] > 0) and np.all(res["photons"] > 0)
+    photons, steps, waves = s.stats()
+    assert photons == int(res["photons"].sum()) and waves > 0
+    s.close()

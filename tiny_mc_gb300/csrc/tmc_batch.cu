@@ -26,35 +26,11 @@
 #include <memory>
 #include <vector>
 
+#include "tmc_batch.cuh"
 #include "tmc_internal.h"
 #include "tmc_walk.cuh"
 
 namespace tmc {
-
-constexpr int BATCH_CHUNK = 32;   // photon ids a warp claims from its item at once
-
-struct BatchProblemDev {
-    WalkConsts c;
-    unsigned long long id_base;
-    unsigned long long tally_offset;   // in shells
-};
-
-struct BatchItemDev {
-    uint32_t problem;
-    uint32_t count;
-    unsigned long long first;          // first photon of the item, relative to the problem
-};
-
-struct BatchArgs {
-    PhiloxKeys keys;
-    const BatchProblemDev *problems;
-    const BatchItemDev *items;
-    uint32_t n_items;
-    uint32_t max_shells;
-    unsigned long long *tally;         // [total shells][4]
-    unsigned long long *steps;         // [problems]
-    unsigned long long *item_counter;  // zero at launch
-};
 
 template <int BLOCK, class M>
 __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
@@ -88,11 +64,77 @@ __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
 
         __syncthreads();
         flush_tally<BLOCK>(smem, S, g);
+        if (a.item_probe && threadIdx.x == 0) {
+            // this item's own sum of w in the probe shell (its 64-bit shared
+            // sum cannot wrap: the planner bounds the item's total weight)
+            const uint32_t ps = min(a.probe_shell, S - 1);
+            a.item_probe[it] = ((unsigned long long)smem[S + ps] << 32) | smem[ps];
+        }
         const unsigned long long tot = warp_sum_u64(steps);
         if ((threadIdx.x & 31u) == 0 && tot)
             atomicAdd(&a.steps[item.problem], tot);
         __syncthreads();
     }
+}
+
+template <int BLOCK, class M>
+static cudaError_t walk_batch_config(int sms, size_t smem, int *grid)
+{
+    auto kern = walk_batch<BLOCK, M>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, smem);
+    if (e != cudaSuccess)
+        return e;
+    if (per_sm < 1)
+        return cudaErrorInvalidConfiguration;
+    *grid = sms * per_sm;
+    return cudaSuccess;
+}
+
+size_t walk_batch_smem(uint32_t max_shells, int block)
+{
+    return (size_t)16 * max_shells + (size_t)4 * SLOTS * block;
+}
+
+cudaError_t walk_batch_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid)
+{
+    const size_t smem = walk_batch_smem(max_shells, block);
+    const bool fast = math == TMC_MATH_FAST;
+    switch (block) {
+    case 128: return fast ? walk_batch_config<128, FastMath>(sms, smem, grid)
+                          : walk_batch_config<128, ExactMath>(sms, smem, grid);
+    case 256: return fast ? walk_batch_config<256, FastMath>(sms, smem, grid)
+                          : walk_batch_config<256, ExactMath>(sms, smem, grid);
+    case 512: return fast ? walk_batch_config<512, FastMath>(sms, smem, grid)
+                          : walk_batch_config<512, ExactMath>(sms, smem, grid);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t walk_batch_launch(const BatchArgs &a, int block, uint32_t math, int grid, cudaStream_t s)
+{
+    const size_t smem = walk_batch_smem(a.max_shells, block);
+    const bool fast = math == TMC_MATH_FAST;
+    switch (block) {
+    case 128:
+        if (fast) walk_batch<128, FastMath><<<grid, 128, smem, s>>>(a);
+        else walk_batch<128, ExactMath><<<grid, 128, smem, s>>>(a);
+        break;
+    case 256:
+        if (fast) walk_batch<256, FastMath><<<grid, 256, smem, s>>>(a);
+        else walk_batch<256, ExactMath><<<grid, 256, smem, s>>>(a);
+        break;
+    case 512:
+        if (fast) walk_batch<512, FastMath><<<grid, 512, smem, s>>>(a);
+        else walk_batch<512, ExactMath><<<grid, 512, smem, s>>>(a);
+        break;
+    default:
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 
 namespace {
@@ -153,41 +195,11 @@ struct tmc_batch {
 
 namespace {
 
-template <int BLOCK, class M>
-cudaError_t batch_kernel_config(int sms, size_t smem, int *grid)
-{
-    auto kern = walk_batch<BLOCK, M>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess)
-        return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, smem);
-    if (e != cudaSuccess)
-        return e;
-    if (per_sm < 1)
-        return cudaErrorInvalidConfiguration;
-    *grid = sms * per_sm;
-    return cudaSuccess;
-}
-
-size_t batch_smem(const tmc_batch *b, int block)
-{
-    return (size_t)16 * b->max_shells + (size_t)4 * SLOTS * block;
-}
+size_t batch_smem(const tmc_batch *b, int block) { return walk_batch_smem(b->max_shells, block); }
 
 cudaError_t grid_for(const tmc_batch *b, int *grid)
 {
-    const size_t smem = batch_smem(b, b->cfg.block);
-    const bool fast = b->math == TMC_MATH_FAST;
-    switch (b->cfg.block) {
-    case 128: return fast ? batch_kernel_config<128, FastMath>(b->sms, smem, grid)
-                          : batch_kernel_config<128, ExactMath>(b->sms, smem, grid);
-    case 256: return fast ? batch_kernel_config<256, FastMath>(b->sms, smem, grid)
-                          : batch_kernel_config<256, ExactMath>(b->sms, smem, grid);
-    case 512: return fast ? batch_kernel_config<512, FastMath>(b->sms, smem, grid)
-                          : batch_kernel_config<512, ExactMath>(b->sms, smem, grid);
-    default: return cudaErrorInvalidValue;
-    }
+    return walk_batch_prepare(b->cfg.block, b->math, b->max_shells, b->sms, grid);
 }
 
 // Split problems into items of about equal estimated photon steps.
@@ -253,26 +265,6 @@ int plan(tmc_batch *b)
     return TMC_OK;
 }
 
-// Launch only (no attribute calls, so it can be captured): plan() has set
-// the kernel's shared-memory limit and the resident grid.
-template <int BLOCK, class M>
-cudaError_t launch_batch_t(const tmc_batch *b, cudaStream_t s)
-{
-    const size_t smem = batch_smem(b, BLOCK);
-    const int grid = std::max(1, std::min<int>(b->grid, (int)b->n_items));
-    BatchArgs a;
-    a.keys = make_philox_keys(b->seed);
-    a.problems = b->d_problems;
-    a.items = b->d_items;
-    a.n_items = b->n_items;
-    a.max_shells = b->max_shells;
-    a.tally = b->d_tally;
-    a.steps = b->d_steps;
-    a.item_counter = b->d_counter;
-    walk_batch<BLOCK, M><<<grid, BLOCK, smem, s>>>(a);
-    return cudaGetLastError();
-}
-
 cudaError_t enqueue(const tmc_batch *b, cudaStream_t s)
 {
     const size_t n = b->problems.size();
@@ -283,13 +275,21 @@ cudaError_t enqueue(const tmc_batch *b, cudaStream_t s)
         e = cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess || b->n_items == 0)
         return e;
-    const bool fast = b->math == TMC_MATH_FAST;
-    switch (b->cfg.block) {
-    case 128: return fast ? launch_batch_t<128, FastMath>(b, s) : launch_batch_t<128, ExactMath>(b, s);
-    case 256: return fast ? launch_batch_t<256, FastMath>(b, s) : launch_batch_t<256, ExactMath>(b, s);
-    case 512: return fast ? launch_batch_t<512, FastMath>(b, s) : launch_batch_t<512, ExactMath>(b, s);
-    default: return cudaErrorInvalidValue;
-    }
+    // launch only (no attribute calls, so it can be captured): plan() has set
+    // the kernel's shared-memory limit and the resident grid
+    BatchArgs a;
+    a.keys = make_philox_keys(b->seed);
+    a.problems = b->d_problems;
+    a.items = b->d_items;
+    a.n_items = b->n_items;
+    a.max_shells = b->max_shells;
+    a.probe_shell = 0;
+    a.tally = b->d_tally;
+    a.steps = b->d_steps;
+    a.item_counter = b->d_counter;
+    a.item_probe = nullptr;
+    const int grid = std::max(1, std::min<int>(b->grid, (int)b->n_items));
+    return walk_batch_launch(a, b->cfg.block, b->math, grid, s);
 }
 
 int check_batch_device(const tmc_batch *b)

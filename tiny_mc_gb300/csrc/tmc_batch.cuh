@@ -1,0 +1,45 @@
+// tmc_batch.cuh — the batched walk kernel's tables and launch helpers, shared
+// by the batch plan (tmc_batch.cu) and the request server (tmc_serve.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "tmc_walk.cuh"
+
+namespace tmc {
+
+constexpr int BATCH_CHUNK = 32;   // photon ids a warp claims from its item at once
+
+struct BatchProblemDev {
+    WalkConsts c;
+    unsigned long long id_base;
+    unsigned long long tally_offset;   // in shells
+};
+
+struct BatchItemDev {
+    uint32_t problem;
+    uint32_t count;
+    unsigned long long first;          // first photon of the item, relative to the problem
+};
+
+struct BatchArgs {
+    PhiloxKeys keys;
+    const BatchProblemDev *problems;
+    const BatchItemDev *items;
+    uint32_t n_items;
+    uint32_t max_shells;
+    uint32_t probe_shell;              // shell whose per-item sum goes to item_probe
+    unsigned long long *tally;         // [total shells][4]
+    unsigned long long *steps;         // [problems]
+    unsigned long long *item_counter;  // zero at launch
+    unsigned long long *item_probe;    // [n_items] or null
+};
+
+size_t walk_batch_smem(uint32_t max_shells, int block);
+// Sets the kernel's shared-memory limit and returns the resident grid.
+cudaError_t walk_batch_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid);
+// Launch only (capturable); walk_batch_prepare must have run for this shape.
+cudaError_t walk_batch_launch(const BatchArgs &a, int block, uint32_t math, int grid, cudaStream_t s);
+
+}  // namespace tmc

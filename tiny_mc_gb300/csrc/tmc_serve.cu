@@ -1,0 +1,597 @@
+// tmc_serve.cu — a request server for the photon walk: continuous batching of
+// simulation requests that each stop at a target relative standard error.
+//
+// A request is one set of params.h knobs (what tiny_mc.c:34-69 computes for
+// one -D setting) plus a target relative standard error (RSE) of the heat in
+// one probe shell and a photon cap.  The server:
+//
+//  * admits a request into a free slot (the slot is its device tally memory,
+//    max_shells x 32 bytes) or refuses it with TMC_E_BUSY, so the caller
+//    queues; the tally and RNG state never leave the device while it runs;
+//  * walks a request in RSE batches of B photons (B a power of two chosen so
+//    one batch is about `steps_per_batch` photon steps, and small enough that
+//    one batch's 64-bit shared sum of a shell cannot wrap).  One batch is one
+//    work item of the batched kernel, walked by one block, which also writes
+//    the batch's own sum of w in the probe shell;
+//  * stops a request only at fixed batch counts (min_batches, then doubling):
+//    there it computes the batch-means RSE of the probe shell in FP64 over
+//    batches 0..k-1 in order, and stops if RSE <= target or the cap is
+//    reached.  The decision depends only on the request's own photons, so a
+//    request's result is the same alone and in any mix;
+//  * runs work in waves: one launch of the batched kernel over the next
+//    batches of every active request, with two waves in flight on two
+//    streams, so requests that arrive while a wave runs are admitted and
+//    their work starts in the next wave while the previous one is still on
+//    the device.  A request is in at most one wave at a time.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "tmc_batch.cuh"
+#include "tmc_internal.h"
+
+using namespace tmc;
+
+namespace {
+
+constexpr int WAVES = 2;
+using Clock = std::chrono::steady_clock;
+
+double now_s()
+{
+    return std::chrono::duration<double>(Clock::now().time_since_epoch()).count();
+}
+
+struct Req {
+    uint64_t id = 0;
+    tmc_request r{};
+    Derived d{};
+    int slot = -1;
+    uint32_t batch = 0;             // photons per RSE batch
+    uint64_t max_batches = 0;
+    uint64_t issued = 0, done = 0;  // batches
+    uint64_t next_decision = 0;
+    std::vector<double> x;          // per-batch sum of w in the probe shell (2^-40 units)
+    bool in_flight = false;
+    double t_submit = 0.0;
+};
+
+struct Wave {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    BatchItemDev *d_items = nullptr;
+    unsigned long long *d_probe = nullptr;
+    unsigned long long *d_counter = nullptr;
+    BatchItemDev *h_items = nullptr;        // pinned
+    unsigned long long *h_probe = nullptr;  // pinned
+    uint32_t n_items = 0;
+    bool busy = false;
+    std::vector<uint64_t> reqs;             // request ids in this wave
+};
+
+struct Done {
+    tmc_request_result res{};
+    std::vector<tmc_tally> tally;
+};
+
+}  // namespace
+
+struct tmc_server {
+    tmc_server_config cfg{};
+    int device = -1, sms = 0, grid = 0;
+    uint32_t items_cap = 0;
+    BatchProblemDev *d_problems = nullptr;
+    unsigned long long *d_tally = nullptr;   // [slots][max_shells][4]
+    unsigned long long *d_steps = nullptr;   // [slots]
+    cudaStream_t admin = nullptr;
+    Wave waves[WAVES];
+    std::vector<int> free_slots;
+    std::unordered_map<uint64_t, Req> active;
+    std::deque<uint64_t> order;              // admission order of active requests
+    std::unordered_map<uint64_t, Done> finished;
+    uint64_t next_id = 1;
+    uint64_t photons = 0, steps = 0, n_waves = 0;
+    PhiloxKeys keys{};
+};
+
+namespace {
+
+void destroy_server(tmc_server *s)
+{
+    if (!s)
+        return;
+    for (Wave &w : s->waves) {
+        if (w.stream)
+            cudaStreamSynchronize(w.stream);
+        if (w.done)
+            cudaEventDestroy(w.done);
+        if (w.stream)
+            cudaStreamDestroy(w.stream);
+        cudaFree(w.d_items);
+        cudaFree(w.d_probe);
+        cudaFree(w.d_counter);
+        cudaFreeHost(w.h_items);
+        cudaFreeHost(w.h_probe);
+    }
+    if (s->admin)
+        cudaStreamDestroy(s->admin);
+    cudaFree(s->d_problems);
+    cudaFree(s->d_tally);
+    cudaFree(s->d_steps);
+    delete s;
+}
+
+// Photons per RSE batch: a power of two near steps_per_batch / E[steps],
+// in [32, 8192], and at most 2^24 (1 - albedo): a photon deposits at most
+// 1/(1-albedo) weight units, so a batch's shell sum stays below 2^64
+// fixed-point units and its 64-bit shared sum cannot wrap.
+uint32_t batch_photons(const tmc_server_config &cfg, const Derived &d, double est_steps)
+{
+    double want = cfg.steps_per_batch / std::max(1.0, est_steps);
+    uint32_t b = 32;
+    while (b < 8192 && 2.0 * b <= want)
+        b *= 2;
+    const double bound = std::floor(16777216.0 * (1.0 - (double)d.albedo));
+    while (b > 1 && (double)b > bound)
+        b /= 2;
+    return b;
+}
+
+double expected_steps_host(float albedo)
+{
+    if (!(albedo > 0.0f))
+        return 1.0 / 0.9;
+    const double la = std::log((double)albedo);
+    double w = 1.0, e = 0.0, p = 1.0;
+    for (int stage = 0; stage < 12 && p > 1e-12; ++stage) {
+        double k = std::max(1.0, std::ceil(std::log(0.001 / w) / la));
+        e += p * k;
+        w = w * std::pow((double)albedo, k) / 0.1;
+        p *= 0.1;
+    }
+    return e;
+}
+
+// batch-means RSE of x[0..k)
+double batch_rse(const std::vector<double> &x, uint64_t k, double *mean_out)
+{
+    double sum = 0.0;
+    for (uint64_t j = 0; j < k; ++j)
+        sum += x[j];
+    const double m = sum / (double)k;
+    double ss = 0.0;
+    for (uint64_t j = 0; j < k; ++j)
+        ss += (x[j] - m) * (x[j] - m);
+    *mean_out = m;
+    if (!(m > 0.0) || k < 2)
+        return NAN;
+    return std::sqrt(ss / (double)(k - 1) / (double)k) / m;
+}
+
+int finish(tmc_server *s, Req &q, bool reached, double rse)
+{
+    Done dn;
+    dn.tally.resize(q.r.shells);
+    unsigned long long st = 0;
+    cudaError_t e = cudaMemcpy(dn.tally.data(), s->d_tally + 4ull * q.slot * s->cfg.max_shells,
+                               sizeof(tmc_tally) * q.r.shells, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(&st, s->d_steps + q.slot, sizeof st, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "server result copy");
+    dn.res.photons = q.done * (uint64_t)q.batch;
+    dn.res.photon_steps = st;
+    dn.res.batches = (uint32_t)q.done;
+    dn.res.batch_photons = q.batch;
+    dn.res.rse = rse;
+    dn.res.reached_target = reached ? 1 : 0;
+    dn.res.latency_s = now_s() - q.t_submit;
+    s->photons += dn.res.photons;
+    s->steps += st;
+    s->finished[q.id] = std::move(dn);
+    s->free_slots.push_back(q.slot);
+    return TMC_OK;
+}
+
+// Harvest a completed wave: record per-batch values, decide at decision points.
+int harvest(tmc_server *s, Wave &w)
+{
+    // map slot -> request for this wave
+    std::unordered_map<int, Req *> by_slot;
+    for (uint64_t id : w.reqs) {
+        auto f = s->active.find(id);
+        if (f != s->active.end())
+            by_slot[f->second.slot] = &f->second;
+    }
+    for (uint32_t i = 0; i < w.n_items; ++i) {
+        const BatchItemDev &it = w.h_items[i];
+        Req *q = by_slot[(int)it.problem];
+        const uint64_t j = it.first / q->batch;
+        q->x[j] = (double)w.h_probe[i] * 0x1p-40;
+        ++q->done;
+    }
+    for (uint64_t id : w.reqs) {
+        auto f = s->active.find(id);
+        if (f == s->active.end())
+            continue;
+        Req &q = f->second;
+        q.in_flight = false;
+        if (q.done == q.next_decision && q.issued == q.done) {
+            double m = 0.0;
+            const double rse = batch_rse(q.x, q.done, &m);
+            const bool reached = (rse == rse) && rse <= q.r.target_rse;
+            if (reached || q.done >= q.max_batches) {
+                int st = finish(s, q, reached, rse);
+                if (st)
+                    return st;
+                s->order.erase(std::find(s->order.begin(), s->order.end(), id));
+                s->active.erase(f);
+            } else {
+                q.next_decision = std::min(2 * q.done, q.max_batches);
+            }
+        }
+    }
+    w.busy = false;
+    w.reqs.clear();
+    w.n_items = 0;
+    return TMC_OK;
+}
+
+int launch_wave(tmc_server *s, Wave &w)
+{
+    uint32_t n = 0;
+    w.reqs.clear();
+    for (uint64_t id : s->order) {
+        Req &q = s->active[id];
+        if (q.in_flight || q.issued >= q.next_decision)
+            continue;
+        const uint64_t k = std::min<uint64_t>(q.next_decision - q.issued, s->cfg.max_items_per_request);
+        if (n + k > s->items_cap)
+            break;
+        for (uint64_t j = 0; j < k; ++j) {
+            BatchItemDev &it = w.h_items[n++];
+            it.problem = (uint32_t)q.slot;
+            it.count = q.batch;
+            it.first = (q.issued + j) * (uint64_t)q.batch;
+        }
+        q.issued += k;
+        q.x.resize(q.issued, 0.0);
+        q.in_flight = true;
+        w.reqs.push_back(id);
+    }
+    if (n == 0)
+        return TMC_OK;
+    w.n_items = n;
+    cudaError_t e = cudaMemcpyAsync(w.d_items, w.h_items, sizeof(BatchItemDev) * n,
+                                    cudaMemcpyHostToDevice, w.stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(w.d_counter, 0, sizeof(unsigned long long), w.stream);
+    if (e == cudaSuccess) {
+        BatchArgs a;
+        a.keys = s->keys;
+        a.problems = s->d_problems;
+        a.items = w.d_items;
+        a.n_items = n;
+        a.max_shells = s->cfg.max_shells;
+        a.probe_shell = s->cfg.probe_shell;
+        a.tally = s->d_tally;
+        a.steps = s->d_steps;
+        a.item_counter = w.d_counter;
+        a.item_probe = w.d_probe;
+        e = walk_batch_launch(a, (int)s->cfg.block, s->cfg.math, std::max(1, std::min<int>(s->grid, (int)n)),
+                              w.stream);
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(w.h_probe, w.d_probe, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost,
+                            w.stream);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(w.done, w.stream);
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "server wave launch");
+    w.busy = true;
+    ++s->n_waves;
+    return TMC_OK;
+}
+
+int progress_locked(tmc_server *s)
+{
+    for (Wave &w : s->waves) {
+        if (!w.busy)
+            continue;
+        cudaError_t e = cudaEventQuery(w.done);
+        if (e == cudaErrorNotReady)
+            continue;
+        if (e != cudaSuccess)
+            return set_cuda_error(e, "server wave");
+        int st = harvest(s, w);
+        if (st)
+            return st;
+    }
+    for (Wave &w : s->waves) {
+        if (w.busy)
+            continue;
+        int st = launch_wave(s, w);
+        if (st)
+            return st;
+    }
+    return TMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void tmc_server_config_default(tmc_server_config *c)
+{
+    if (!c)
+        return;
+    std::memset(c, 0, sizeof *c);
+    c->slots = 1024;
+    c->max_shells = 501;
+    c->probe_shell = 10;
+    c->min_batches = 32;
+    c->seed = 1;
+    c->math = TMC_MATH_FAST;
+    c->block = 128;
+    c->max_items_per_request = 1024;
+    c->steps_per_batch = 2097152.0;
+}
+
+int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
+{
+    if (!out || !cfg)
+        return TMC_E_INVALID;
+    *out = nullptr;
+    if (cfg->slots == 0 || cfg->slots > (1u << 20) || cfg->max_shells == 0 ||
+        cfg->max_shells > (1u << 16) || cfg->min_batches < 2 || cfg->max_items_per_request == 0 ||
+        !(cfg->steps_per_batch > 0.0) || (cfg->math != TMC_MATH_EXACT && cfg->math != TMC_MATH_FAST) ||
+        (cfg->block != 128 && cfg->block != 256 && cfg->block != 512))
+        return TMC_E_INVALID;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    int st = TMC_OK;
+    DeviceCtx *c = current_ctx(&st);
+    if (!c)
+        return st;
+    std::unique_ptr<tmc_server, void (*)(tmc_server *)> s(new tmc_server, destroy_server);
+    s->cfg = *cfg;
+    s->device = c->device;
+    s->sms = c->sms;
+    s->keys = make_philox_keys(cfg->seed);
+    if (walk_batch_smem(cfg->max_shells, (int)cfg->block) > c->smem_optin) {
+        set_error_text("tmc_server_create: max_shells too large for the shared-memory histogram");
+        return TMC_E_INVALID;
+    }
+    cudaError_t e = walk_batch_prepare((int)cfg->block, cfg->math, cfg->max_shells, c->sms, &s->grid);
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "server kernel config");
+    const size_t slots = cfg->slots;
+    s->items_cap = (uint32_t)std::min<uint64_t>(1u << 22, (uint64_t)slots * cfg->max_items_per_request);
+    e = cudaMalloc(&s->d_problems, sizeof(BatchProblemDev) * slots);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&s->d_tally, sizeof(tmc_tally) * slots * cfg->max_shells);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&s->d_steps, sizeof(unsigned long long) * slots);
+    if (e == cudaSuccess)
+        e = cudaStreamCreateWithFlags(&s->admin, cudaStreamNonBlocking);
+    for (Wave &w : s->waves) {
+        if (e == cudaSuccess)
+            e = cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&w.d_items, sizeof(BatchItemDev) * s->items_cap);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&w.d_probe, sizeof(unsigned long long) * s->items_cap);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&w.d_counter, sizeof(unsigned long long));
+        if (e == cudaSuccess)
+            e = cudaMallocHost(&w.h_items, sizeof(BatchItemDev) * s->items_cap);
+        if (e == cudaSuccess)
+            e = cudaMallocHost(&w.h_probe, sizeof(unsigned long long) * s->items_cap);
+    }
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "tmc_server_create");
+    for (int i = (int)slots - 1; i >= 0; --i)
+        s->free_slots.push_back(i);
+    *out = s.release();
+    return TMC_OK;
+}
+
+int tmc_server_submit(tmc_server *s, const tmc_request *r, uint64_t *id)
+{
+    if (!s || !r)
+        return TMC_E_INVALID;
+    tmc_params p;
+    tmc_params_default(&p);
+    p.shells = r->shells;
+    p.microns_per_shell = r->microns_per_shell;
+    p.mu_a = r->mu_a;
+    p.mu_s = r->mu_s;
+    int st = validate(&p);
+    if (st)
+        return st;
+    if (r->shells > s->cfg.max_shells || !(r->target_rse > 0.0) || r->max_photons == 0 ||
+        r->max_photons > (1ull << 40) || r->photon_id_base > ~0ull - r->max_photons)
+        return TMC_E_INVALID;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    if (s->free_slots.empty())
+        return TMC_E_BUSY;
+    Req q;
+    q.id = s->next_id++;
+    q.r = *r;
+    q.d = derive(r->mu_a, r->mu_s, r->microns_per_shell, r->shells);
+    q.batch = batch_photons(s->cfg, q.d, expected_steps_host(q.d.albedo));
+    q.max_batches = std::max<uint64_t>(1, (r->max_photons + q.batch - 1) / q.batch);
+    q.next_decision = std::min<uint64_t>(s->cfg.min_batches, q.max_batches);
+    q.slot = s->free_slots.back();
+    q.t_submit = now_s();
+    BatchProblemDev pd;
+    pd.c.albedo = q.d.albedo;
+    pd.c.spm = q.d.spm;
+    pd.c.last = q.d.last;
+    pd.c.shells = q.d.shells;
+    pd.id_base = r->photon_id_base;
+    pd.tally_offset = (unsigned long long)q.slot * s->cfg.max_shells;
+    cudaError_t e = cudaMemcpyAsync(s->d_problems + q.slot, &pd, sizeof pd, cudaMemcpyHostToDevice, s->admin);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(s->d_tally + 4ull * q.slot * s->cfg.max_shells, 0,
+                            sizeof(tmc_tally) * s->cfg.max_shells, s->admin);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(s->d_steps + q.slot, 0, sizeof(unsigned long long), s->admin);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s->admin);
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "tmc_server_submit");
+    s->free_slots.pop_back();
+    if (id)
+        *id = q.id;
+    s->order.push_back(q.id);
+    s->active.emplace(q.id, std::move(q));
+    return TMC_OK;
+}
+
+int tmc_server_progress(tmc_server *s, uint32_t *waves_in_flight, uint32_t *active_requests)
+{
+    if (!s)
+        return TMC_E_INVALID;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    int st = progress_locked(s);
+    if (waves_in_flight) {
+        uint32_t n = 0;
+        for (const Wave &w : s->waves)
+            n += w.busy ? 1 : 0;
+        *waves_in_flight = n;
+    }
+    if (active_requests)
+        *active_requests = (uint32_t)s->active.size();
+    return st;
+}
+
+int tmc_server_poll(tmc_server *s, uint64_t id, int *done)
+{
+    if (!s || !done)
+        return TMC_E_INVALID;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    if (s->finished.count(id)) {
+        *done = 1;
+        return TMC_OK;
+    }
+    if (s->active.count(id)) {
+        *done = 0;
+        return TMC_OK;
+    }
+    return TMC_E_STATE;
+}
+
+int tmc_server_result(tmc_server *s, uint64_t id, tmc_tally *tally, tmc_request_result *res)
+{
+    if (!s)
+        return TMC_E_INVALID;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    auto f = s->finished.find(id);
+    if (f == s->finished.end())
+        return TMC_E_STATE;
+    if (tally)
+        std::memcpy(tally, f->second.tally.data(), sizeof(tmc_tally) * f->second.tally.size());
+    if (res)
+        *res = f->second.res;
+    s->finished.erase(f);
+    return TMC_OK;
+}
+
+int tmc_server_stats(tmc_server *s, uint64_t *photons, uint64_t *photon_steps, uint64_t *waves)
+{
+    if (!s)
+        return TMC_E_INVALID;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    if (photons)
+        *photons = s->photons;
+    if (photon_steps)
+        *photon_steps = s->steps;
+    if (waves)
+        *waves = s->n_waves;
+    return TMC_OK;
+}
+
+int tmc_server_run_trace(tmc_server *s, const tmc_request *reqs, const double *arrival_s, uint32_t n,
+                         double time_limit_s, tmc_request_result *results, uint32_t *completed)
+{
+    if (!s || (n && (!reqs || !arrival_s || !results)))
+        return TMC_E_INVALID;
+    for (uint32_t i = 1; i < n; ++i)
+        if (arrival_s[i] < arrival_s[i - 1])
+            return TMC_E_INVALID;
+    std::vector<uint64_t> ids(n, 0);
+    std::unordered_map<uint64_t, uint32_t> index;
+    std::unordered_map<uint64_t, double> submit_t;
+    for (uint32_t i = 0; i < n; ++i)
+        std::memset(&results[i], 0, sizeof results[i]);
+    const double t0 = now_s();
+    uint32_t next = 0, done = 0;
+    int st = TMC_OK;
+    while (done < n) {
+        const double t = now_s() - t0;
+        if (time_limit_s > 0.0 && t > time_limit_s)
+            break;
+        // admit everything that has arrived, in order, while slots are free
+        while (next < n && arrival_s[next] <= t) {
+            uint64_t id = 0;
+            st = tmc_server_submit(s, &reqs[next], &id);
+            if (st == TMC_E_BUSY)
+                break;
+            if (st)
+                return st;
+            ids[next] = id;
+            index[id] = next;
+            submit_t[id] = s->active.count(id) ? s->active[id].t_submit : now_s();
+            ++next;
+        }
+        uint32_t in_flight = 0, act = 0;
+        if ((st = tmc_server_progress(s, &in_flight, &act)))
+            return st;
+        // collect completions
+        std::vector<uint64_t> fin;
+        {
+            std::lock_guard<std::mutex> lk(api_mutex());
+            for (auto &kv : s->finished)
+                if (index.count(kv.first))
+                    fin.push_back(kv.first);
+        }
+        for (uint64_t id : fin) {
+            const uint32_t i = index[id];
+            tmc_request_result r;
+            if ((st = tmc_server_result(s, id, nullptr, &r)))
+                return st;
+            // latency from arrival, not from admission: completion time is
+            // submission time + the server's latency
+            const double t_sub = (double)(submit_t.count(id) ? submit_t[id] : t0);
+            r.latency_s = (t_sub + r.latency_s) - (t0 + arrival_s[i]);
+            submit_t.erase(id);
+            results[i] = r;
+            index.erase(id);
+            ++done;
+        }
+        if (fin.empty())
+            std::this_thread::sleep_for(std::chrono::microseconds(in_flight ? 20 : 200));
+    }
+    if (completed)
+        *completed = done;
+    return TMC_OK;
+}
+
+int tmc_server_destroy(tmc_server *s)
+{
+    if (!s)
+        return TMC_OK;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    destroy_server(s);
+    return TMC_OK;
+}
+
+}  // extern "C"
