@@ -56,8 +56,14 @@ def parse():
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=["plain", "sweep"], default="plain",
-                    help="plain: config 1 (default); sweep: the 4096-problem batched sweep")
+    ap.add_argument("--workload", choices=["plain", "sweep", "serve"], default="plain",
+                    help="plain: config 1 (default); sweep: the 4096-problem batched sweep; "
+                         "serve: the request stream")
+    ap.add_argument("--serve-slots", type=int, default=1024)
+    ap.add_argument("--serve-calib", type=int, default=256)
+    ap.add_argument("--serve-window", type=float, default=10.0)
+    ap.add_argument("--serve-duration", type=float, default=60.0)
+    ap.add_argument("--serve-drain", type=float, default=120.0)
     ap.add_argument("--sweep-scale", type=float, default=1.0 / 64,
                     help="photon-count multiplier of the sweep (1 = full size, ~3.3e13 steps)")
     ap.add_argument("--plain-steps", type=int, default=1,
@@ -425,7 +431,7 @@ def run_sweep(args):
                         photon_id_base=int(q["photon_id_base"]), math=args.math) for q in sw]
     sp = stream.cuda_stream
     plain_ms = []
-    for _ in range(max(1, args.plain_steps)):
+    for _ in range(args.plain_steps):
         a_, c_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a_.record(stream)
         for q, p in zip(sw, plist):
@@ -433,7 +439,7 @@ def run_sweep(args):
         c_.record(stream)
         torch.cuda.synchronize()
         plain_ms.append(a_.elapsed_time(c_))
-    plain = photons * len(plain_ms) / (sum(plain_ms) * 1e-3)
+    plain = photons * len(plain_ms) / (sum(plain_ms) * 1e-3) if plain_ms else None
     n_items, _ = b.info()
     line = {
         "metric": METRIC, "value": batched, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
@@ -446,12 +452,96 @@ def run_sweep(args):
                    "sweep_seed": 0, "rng_seed": 1, "batch_config": b.config(), "work_items": n_items,
                    "autotune_s": tune_s, "autotune_best_ms": tune_ms},
         "photon_steps_per_s": photon_steps * args.steps / (sum(ms) * 1e-3),
-        "plain_form": {"value": plain, "unit": UNIT, "ms_per_pass": sum(plain_ms) / len(plain_ms),
-                       "launches_per_pass": len(sw)},
-        "batched_over_plain": batched / plain,
+        "plain_form": ({"value": plain, "unit": UNIT, "ms_per_pass": sum(plain_ms) / len(plain_ms),
+                        "launches_per_pass": len(sw)} if plain_ms else None),
+        "batched_over_plain": batched / plain if plain else None,
         "gpu_launches": args.steps, "clocks": clk,
     }
     b.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_serve(args):
+    """Config 4: Poisson arrivals of requests with the sweep's parameter
+    distribution, a target RSE at shell 10 in [0.5 %, 5 %] and a 2^24-photon
+    cap.  Three measurements on one server:
+      1. calibration: the first requests of the trace submitted at once give
+         the mean photon steps per request and the server's throughput, hence
+         the offered load of the configured rate (2000/s) against capacity;
+      2. the configured rate for a fixed window (no drain): throughput and
+         the latency of what completed while the queue grows;
+      3. the same trace with arrivals slowed to 70 % of capacity: p50/p99
+         latency of a stream the GPU can sustain."""
+    import numpy as np
+    import torch
+
+    from tiny_mc_gb300.serve import Server, make_trace
+
+    torch.cuda.set_device(0)
+    n_total = 100000
+    req, arr = make_trace(n_total, rate=2000.0, seed=0)
+    s = Server(slots=args.serve_slots, math=1 if args.math == "fast" else 0)
+    # 1. calibration
+    C = args.serve_calib
+    t0 = time.perf_counter()
+    res_c, done_c = s.run_trace(req[:C], np.zeros(C), time_limit_s=600.0)
+    t_c = time.perf_counter() - t0
+    calib_steps = float(res_c["photon_steps"].sum())
+    mean_steps = calib_steps / max(1, done_c)
+    capacity = calib_steps / t_c
+    offered = 2000.0 * mean_steps / capacity
+    # 2. configured rate, fixed window
+    W = args.serve_window
+    sel = slice(C, C + int(2000.0 * W * 1.2))
+    a2 = arr[sel] - arr[sel][0]
+    clocks = ClockSampler(None)
+    clocks.start()
+    t0 = time.perf_counter()
+    res_o, done_o = s.run_trace(req[sel], a2, time_limit_s=W)
+    t_o = time.perf_counter() - t0
+    arrived = int(np.sum(a2 <= t_o))
+    got = res_o["photons"] > 0
+    lat_o = res_o["latency_s"][got]
+    s.close()
+    # 3. slowed to 70 % of capacity
+    s = Server(slots=args.serve_slots, math=1 if args.math == "fast" else 0)
+    rate = 0.7 * capacity / mean_steps
+    n3 = max(50, min(int(rate * args.serve_duration), n_total - C))
+    sel3 = slice(C, C + n3)
+    a3 = (arr[sel3] - arr[sel3][0]) * (2000.0 / rate)
+    t0 = time.perf_counter()
+    res_s, done_s = s.run_trace(req[sel3], a3, time_limit_s=a3[-1] + args.serve_drain)
+    t_s = time.perf_counter() - t0
+    clk = clocks.stop()
+    got3 = res_s["photons"] > 0
+    lat = res_s["latency_s"][got3]
+    photons3 = float(res_s["photons"].sum())
+    steps3 = float(res_s["photon_steps"].sum())
+    s.close()
+    pct = lambda v, q: float(np.percentile(v, q)) if len(v) else None  # noqa: E731
+    line = {
+        "metric": METRIC, "value": photons3 / t_s, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 0,
+        "ms_per_step": t_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "served stream (config 4): Poisson arrivals, target RSE at shell 10 "
+                               "in [0.5%, 5%], cap 2^24 photons, sweep parameter distribution",
+                   "trace_seed": 0, "math": args.math, "slots": args.serve_slots},
+        "latency_p50_s": pct(lat, 50), "latency_p99_s": pct(lat, 99),
+        "photon_steps_per_s": steps3 / t_s,
+        "requests": n3, "completed": int(done_s), "arrival_rate_per_s": rate,
+        "reached_target_frac": float(np.mean(res_s["reached_target"][got3])) if got3.any() else None,
+        "calibration": {"requests": C, "mean_photon_steps_per_request": mean_steps,
+                        "capacity_photon_steps_per_s": capacity,
+                        "offered_load_at_2000_per_s": offered},
+        "at_2000_per_s_window": {"window_s": W, "arrived": arrived, "completed": int(done_o),
+                                 "photons_per_s": float(res_o["photons"].sum()) / t_o,
+                                 "photon_steps_per_s_completed": float(res_o["photon_steps"].sum()) / t_o,
+                                 "latency_p50_s_completed": pct(lat_o, 50),
+                                 "latency_p99_s_completed": pct(lat_o, 99),
+                                 "overloaded": bool(offered > 1.0)},
+        "clocks": clk,
+    }
     print(json.dumps(line), flush=True)
     return 0
 
@@ -462,6 +552,8 @@ def main():
         return run_reference(args)
     if args.workload == "sweep":
         return run_sweep(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_ours(args)
 
 

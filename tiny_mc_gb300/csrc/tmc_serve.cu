@@ -9,20 +9,24 @@
 //    max_shells x 32 bytes) or refuses it with TMC_E_BUSY, so the caller
 //    queues; the tally and RNG state never leave the device while it runs;
 //  * walks a request in RSE batches of B photons (B a power of two chosen so
-//    one batch is about `steps_per_batch` photon steps, and small enough that
-//    one batch's 64-bit shared sum of a shell cannot wrap).  One batch is one
-//    work item of the batched kernel, walked by one block, which also writes
-//    the batch's own sum of w in the probe shell;
+//    one batch is about `steps_per_batch` photon steps, at least one photon
+//    per thread of a block).  A batch is one or more work items of the
+//    batched kernel, each walked by one block, which also writes the item's
+//    own sum of w in the probe shell; items are small enough that that 64-bit
+//    shared sum cannot wrap;
 //  * stops a request only at fixed batch counts (min_batches, then doubling):
 //    there it computes the batch-means RSE of the probe shell in FP64 over
 //    batches 0..k-1 in order, and stops if RSE <= target or the cap is
 //    reached.  The decision depends only on the request's own photons, so a
 //    request's result is the same alone and in any mix;
-//  * runs work in waves: one launch of the batched kernel over the next
-//    batches of every active request, with two waves in flight on two
-//    streams, so requests that arrive while a wave runs are admitted and
-//    their work starts in the next wave while the previous one is still on
-//    the device.  A request is in at most one wave at a time.
+//  * runs work in waves: launches of the batched kernel over a bounded
+//    number of pending items, taken round-robin from the active requests,
+//    with up to four waves in flight on four streams.  Requests that arrive
+//    while waves run are admitted and their items join the next wave while
+//    earlier ones are still on the device; a request's items may be spread
+//    over several waves, and its stop decision waits until every item before
+//    the decision point is back.  Batch values are summed from per-item
+//    values in item order, so the decision does not depend on timing.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -40,7 +44,7 @@ using namespace tmc;
 
 namespace {
 
-constexpr int WAVES = 2;
+constexpr int WAVES = 4;
 using Clock = std::chrono::steady_clock;
 
 double now_s()
@@ -54,11 +58,12 @@ struct Req {
     Derived d{};
     int slot = -1;
     uint32_t batch = 0;             // photons per RSE batch
+    uint32_t item_photons = 0;      // photons per work item
+    uint32_t items_per_batch = 0;
     uint64_t max_batches = 0;
-    uint64_t issued = 0, done = 0;  // batches
-    uint64_t next_decision = 0;
-    std::vector<double> x;          // per-batch sum of w in the probe shell (2^-40 units)
-    bool in_flight = false;
+    uint64_t issued = 0, done = 0;  // work items
+    uint64_t next_decision = 0;     // in batches
+    std::vector<unsigned long long> probe;   // per item: sum of w in the probe shell (2^-40 units)
     double t_submit = 0.0;
 };
 
@@ -72,7 +77,6 @@ struct Wave {
     unsigned long long *h_probe = nullptr;  // pinned
     uint32_t n_items = 0;
     bool busy = false;
-    std::vector<uint64_t> reqs;             // request ids in this wave
 };
 
 struct Done {
@@ -94,6 +98,9 @@ struct tmc_server {
     std::vector<int> free_slots;
     std::unordered_map<uint64_t, Req> active;
     std::deque<uint64_t> order;              // admission order of active requests
+    std::vector<uint64_t> slot_req;          // slot -> request id
+    size_t rr = 0;                           // round-robin cursor into order
+    uint32_t wave_cap = 0;                   // items per wave
     std::unordered_map<uint64_t, Done> finished;
     uint64_t next_id = 1;
     uint64_t photons = 0, steps = 0, n_waves = 0;
@@ -127,20 +134,28 @@ void destroy_server(tmc_server *s)
     delete s;
 }
 
-// Photons per RSE batch: a power of two near steps_per_batch / E[steps],
-// in [32, 8192], and at most 2^24 (1 - albedo): a photon deposits at most
-// 1/(1-albedo) weight units, so a batch's shell sum stays below 2^64
-// fixed-point units and its 64-bit shared sum cannot wrap.
-uint32_t batch_photons(const tmc_server_config &cfg, const Derived &d, double est_steps)
+// Photons per RSE batch: a power of two near steps_per_batch / E[steps], in
+// [block, 8192] (at least one photon per thread of the block walking it).
+uint32_t batch_photons(const tmc_server_config &cfg, double est_steps)
 {
-    double want = cfg.steps_per_batch / std::max(1.0, est_steps);
-    uint32_t b = 32;
+    const double want = cfg.steps_per_batch / std::max(1.0, est_steps);
+    uint32_t b = cfg.block;
     while (b < 8192 && 2.0 * b <= want)
         b *= 2;
-    const double bound = std::floor(16777216.0 * (1.0 - (double)d.albedo));
-    while (b > 1 && (double)b > bound)
-        b /= 2;
     return b;
+}
+
+// Photons per work item: the batch, halved until the item is at most
+// 2^24 (1 - albedo) photons.  A photon deposits at most 1/(1-albedo) weight
+// units, so an item's sum in one shell stays below 2^64 fixed-point units and
+// its 64-bit shared sum cannot wrap.
+uint32_t item_photons(uint32_t batch, const Derived &d)
+{
+    const double bound = std::floor(16777216.0 * (1.0 - (double)d.albedo));
+    uint32_t p = batch;
+    while (p > 1 && (double)p > bound)
+        p /= 2;
+    return p;
 }
 
 double expected_steps_host(float albedo)
@@ -158,9 +173,15 @@ double expected_steps_host(float albedo)
     return e;
 }
 
-// batch-means RSE of x[0..k)
-double batch_rse(const std::vector<double> &x, uint64_t k, double *mean_out)
+// batch-means RSE over batches 0..k-1; batch j's value is the sum of its
+// items' probes, in item order
+double batch_rse(const std::vector<unsigned long long> &probe, uint32_t ipb, uint64_t k,
+                 double *mean_out)
 {
+    std::vector<double> x(k, 0.0);
+    for (uint64_t j = 0; j < k; ++j)
+        for (uint32_t i = 0; i < ipb; ++i)
+            x[j] += (double)probe[j * ipb + i] * 0x1p-40;
     double sum = 0.0;
     for (uint64_t j = 0; j < k; ++j)
         sum += x[j];
@@ -185,9 +206,9 @@ int finish(tmc_server *s, Req &q, bool reached, double rse)
         e = cudaMemcpy(&st, s->d_steps + q.slot, sizeof st, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess)
         return set_cuda_error(e, "server result copy");
-    dn.res.photons = q.done * (uint64_t)q.batch;
+    dn.res.photons = q.done * (uint64_t)q.item_photons;
     dn.res.photon_steps = st;
-    dn.res.batches = (uint32_t)q.done;
+    dn.res.batches = (uint32_t)(q.done / q.items_per_batch);
     dn.res.batch_photons = q.batch;
     dn.res.rse = rse;
     dn.res.reached_target = reached ? 1 : 0;
@@ -199,72 +220,88 @@ int finish(tmc_server *s, Req &q, bool reached, double rse)
     return TMC_OK;
 }
 
-// Harvest a completed wave: record per-batch values, decide at decision points.
+// Decide a request whose items up to its decision point are all back.
+int decide(tmc_server *s, uint64_t id)
+{
+    auto f = s->active.find(id);
+    if (f == s->active.end())
+        return TMC_OK;
+    Req &q = f->second;
+    if (q.done != q.next_decision * q.items_per_batch)
+        return TMC_OK;
+    double m = 0.0;
+    const double rse = batch_rse(q.probe, q.items_per_batch, q.next_decision, &m);
+    const bool reached = (rse == rse) && rse <= q.r.target_rse;
+    if (reached || q.next_decision >= q.max_batches) {
+        int st = finish(s, q, reached, rse);
+        if (st)
+            return st;
+        s->order.erase(std::find(s->order.begin(), s->order.end(), id));
+        s->active.erase(f);
+    } else {
+        q.next_decision = std::min(2 * q.next_decision, q.max_batches);
+    }
+    return TMC_OK;
+}
+
+// Harvest a completed wave: store per-item values, decide where possible.
 int harvest(tmc_server *s, Wave &w)
 {
-    // map slot -> request for this wave
-    std::unordered_map<int, Req *> by_slot;
-    for (uint64_t id : w.reqs) {
-        auto f = s->active.find(id);
-        if (f != s->active.end())
-            by_slot[f->second.slot] = &f->second;
-    }
+    std::vector<uint64_t> touched;
     for (uint32_t i = 0; i < w.n_items; ++i) {
         const BatchItemDev &it = w.h_items[i];
-        Req *q = by_slot[(int)it.problem];
-        const uint64_t j = it.first / q->batch;
-        q->x[j] = (double)w.h_probe[i] * 0x1p-40;
-        ++q->done;
+        const uint64_t id = s->slot_req[it.problem];
+        Req &q = s->active[id];
+        q.probe[it.first / q.item_photons] = w.h_probe[i];
+        ++q.done;
+        if (touched.empty() || touched.back() != id)
+            touched.push_back(id);
     }
-    for (uint64_t id : w.reqs) {
-        auto f = s->active.find(id);
-        if (f == s->active.end())
-            continue;
-        Req &q = f->second;
-        q.in_flight = false;
-        if (q.done == q.next_decision && q.issued == q.done) {
-            double m = 0.0;
-            const double rse = batch_rse(q.x, q.done, &m);
-            const bool reached = (rse == rse) && rse <= q.r.target_rse;
-            if (reached || q.done >= q.max_batches) {
-                int st = finish(s, q, reached, rse);
-                if (st)
-                    return st;
-                s->order.erase(std::find(s->order.begin(), s->order.end(), id));
-                s->active.erase(f);
-            } else {
-                q.next_decision = std::min(2 * q.done, q.max_batches);
-            }
-        }
+    std::sort(touched.begin(), touched.end());
+    touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
+    for (uint64_t id : touched) {
+        int st = decide(s, id);
+        if (st)
+            return st;
     }
     w.busy = false;
-    w.reqs.clear();
     w.n_items = 0;
     return TMC_OK;
 }
 
+// Fill a wave with pending items, round-robin over the active requests.
 int launch_wave(tmc_server *s, Wave &w)
 {
     uint32_t n = 0;
-    w.reqs.clear();
+    size_t pending_reqs = 0;
     for (uint64_t id : s->order) {
+        const Req &q = s->active[id];
+        if (q.issued < q.next_decision * q.items_per_batch)
+            ++pending_reqs;
+    }
+    if (pending_reqs == 0)
+        return TMC_OK;
+    const uint64_t quota = std::max<uint64_t>(
+        16, std::min<uint64_t>(s->cfg.max_items_per_request, s->wave_cap / pending_reqs));
+    const size_t m = s->order.size();
+    for (size_t c = 0; c < m && n < s->wave_cap; ++c) {
+        const uint64_t id = s->order[(s->rr + c) % m];
         Req &q = s->active[id];
-        if (q.in_flight || q.issued >= q.next_decision)
+        const uint64_t limit = q.next_decision * q.items_per_batch;
+        if (q.issued >= limit)
             continue;
-        const uint64_t k = std::min<uint64_t>(q.next_decision - q.issued, s->cfg.max_items_per_request);
-        if (n + k > s->items_cap)
-            break;
+        const uint64_t k = std::min<uint64_t>({limit - q.issued, quota, (uint64_t)(s->wave_cap - n)});
         for (uint64_t j = 0; j < k; ++j) {
             BatchItemDev &it = w.h_items[n++];
             it.problem = (uint32_t)q.slot;
-            it.count = q.batch;
-            it.first = (q.issued + j) * (uint64_t)q.batch;
+            it.count = q.item_photons;
+            it.first = (q.issued + j) * (uint64_t)q.item_photons;
         }
         q.issued += k;
-        q.x.resize(q.issued, 0.0);
-        q.in_flight = true;
-        w.reqs.push_back(id);
+        if (q.probe.size() < q.issued)
+            q.probe.resize(q.issued, 0ull);
     }
+    s->rr = m ? (s->rr + 1) % m : 0;
     if (n == 0)
         return TMC_OK;
     w.n_items = n;
@@ -371,7 +408,9 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
     if (e != cudaSuccess)
         return set_cuda_error(e, "server kernel config");
     const size_t slots = cfg->slots;
-    s->items_cap = (uint32_t)std::min<uint64_t>(1u << 22, (uint64_t)slots * cfg->max_items_per_request);
+    s->slot_req.assign(slots, 0);
+    s->wave_cap = (uint32_t)std::max(1024, 4 * s->grid);
+    s->items_cap = s->wave_cap;
     e = cudaMalloc(&s->d_problems, sizeof(BatchProblemDev) * slots);
     if (e == cudaSuccess)
         e = cudaMalloc(&s->d_tally, sizeof(tmc_tally) * slots * cfg->max_shells);
@@ -426,7 +465,9 @@ int tmc_server_submit(tmc_server *s, const tmc_request *r, uint64_t *id)
     q.id = s->next_id++;
     q.r = *r;
     q.d = derive(r->mu_a, r->mu_s, r->microns_per_shell, r->shells);
-    q.batch = batch_photons(s->cfg, q.d, expected_steps_host(q.d.albedo));
+    q.batch = batch_photons(s->cfg, expected_steps_host(q.d.albedo));
+    q.item_photons = item_photons(q.batch, q.d);
+    q.items_per_batch = q.batch / q.item_photons;
     q.max_batches = std::max<uint64_t>(1, (r->max_photons + q.batch - 1) / q.batch);
     q.next_decision = std::min<uint64_t>(s->cfg.min_batches, q.max_batches);
     q.slot = s->free_slots.back();
@@ -449,6 +490,7 @@ int tmc_server_submit(tmc_server *s, const tmc_request *r, uint64_t *id)
     if (e != cudaSuccess)
         return set_cuda_error(e, "tmc_server_submit");
     s->free_slots.pop_back();
+    s->slot_req[q.slot] = q.id;
     if (id)
         *id = q.id;
     s->order.push_back(q.id);
