@@ -147,6 +147,56 @@ int tmc_tally_to_heat(const tmc_tally *tally, const tmc_params *p, double *heat,
 int tmc_format_report(char *buf, size_t cap, const float *heat, const float *heat2,
                       uint64_t photons, const tmc_params *p);
 
+/*
+ * The numbers of that report computed in FP64 on the GPU from exact tallies
+ * (tiny_mc.c:60-66 in double precision): density[i] (W/cm^3) and error[i]
+ * for i < shells-1, and extra = heat[shells-1] / photons.
+ *   tmc_report_fp64_device: d_tally and d_out are device memory; d_out gets
+ *     [density (shells) | error (shells) | extra], asynchronous on stream.
+ *   tmc_report_fp64: host tallies in, host arrays out (density and error of
+ *     shells-1 entries), synchronous.
+ * tmc_format_report_fp64 prints them with the report's printf formats.
+ */
+int tmc_report_fp64_device(const tmc_tally *d_tally, const tmc_params *p, uint64_t photons, double *d_out,
+                           void *stream);
+int tmc_report_fp64(const tmc_tally *tally, const tmc_params *p, uint64_t photons, double *density,
+                    double *error, double *extra);
+int tmc_format_report_fp64(char *buf, size_t cap, const double *density, const double *error,
+                           double extra, const tmc_params *p);
+
+/* ----------------------------------------------------------------- viewer
+ * The viewer's jobs (cg_mc.c) without a graphics stack.  No window, no GL:
+ * a device image buffer.
+ *
+ * tmc_colormap: the fragment shader's arithmetic (cg_mc.c:45-64) per pixel of
+ * a width x height target, row 0 = bottom: shell = int(|uv - 0.5| / 0.7071 *
+ * (shells-1)) with uv = (pixel + 0.5) / 800, red = 2 / (1 + exp(-0.004 *
+ * heats[shell])) - 1.  d_heats (device, float [shells], the viewer's raw
+ * heats array), outputs d_red (float [h][w]) and/or d_rgba (uint8 [h][w][4]).
+ */
+int tmc_colormap(const float *d_heats, uint32_t shells, uint32_t width, uint32_t height, float *d_red,
+                 uint8_t *d_rgba, void *stream);
+/* Same with host arrays (synchronous). */
+int tmc_colormap_host(const float *heats, uint32_t shells, uint32_t width, uint32_t height, float *red,
+                      uint8_t *rgba);
+
+/*
+ * Progressive walk: the viewer's loop (cg_mc.c:71-87, a few photons per frame
+ * into heats, uploaded every frame) as frames that continue the photon-id
+ * sequence, so after k photons the tallies equal one k-photon call.  Each
+ * advance enqueues the frame's walk and an asynchronous snapshot of the
+ * running heat/heat2 (float, like the viewer's arrays); snapshot() copies the
+ * newest finished one without waiting (wait = 0) and returns 1 if it is newer
+ * than the last one returned, else 0.  render() colours the newest device
+ * snapshot into host RGBA8.
+ */
+typedef struct tmc_progressive tmc_progressive;
+int tmc_progressive_create(tmc_progressive **out, const tmc_params *p);
+int tmc_progressive_advance(tmc_progressive *g, uint64_t n_photons);
+int tmc_progressive_snapshot(tmc_progressive *g, float *heat, float *heat2, uint64_t *photons, int wait);
+int tmc_progressive_render(tmc_progressive *g, uint32_t width, uint32_t height, uint8_t *rgba);
+int tmc_progressive_destroy(tmc_progressive *g);
+
 /* ------------------------------------------------------------------ batch
  * Many independent walks in one persistent launch.  Each problem is what the
  * reference computes for one set of params.h knobs (tiny_mc.c:34-69 run with

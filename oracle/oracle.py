@@ -78,6 +78,8 @@ def lib() -> ctypes.CDLL:
         L.tmo_native_run.restype = i32
         L.tmo_native_rate.argtypes = [P, u64, u32, vp]
         L.tmo_native_rate.restype = ctypes.c_double
+        L.tmo_colormap.argtypes = [vp, u32, u32, u32, vp, vp]
+        L.tmo_colormap.restype = None
         _lib = L
     return _lib
 
@@ -181,6 +183,15 @@ def heat_from_tally(p: OParams, tally: np.ndarray):
     sw = t[:, 1] * 2.0 ** 24 + t[:, 0] * 2.0 ** -40
     sw2 = t[:, 3] * 2.0 ** 24 + t[:, 2] * 2.0 ** -40
     return c * sw, c * c * sw2
+
+
+def colormap(heats: np.ndarray, width: int = 800, height: int = 800):
+    """The viewer's colour map (cg_mc.c:38-67): (red float [h, w], rgba uint8 [h, w, 4])."""
+    h = np.ascontiguousarray(heats, np.float32)
+    red = np.zeros((height, width), np.float32)
+    rgba = np.zeros((height, width, 4), np.uint8)
+    lib().tmo_colormap(h.ctypes.data, len(h), width, height, red.ctypes.data, rgba.ctypes.data)
+    return red, rgba
 
 
 # ---------------------------------------------------------------- _ref/

@@ -530,3 +530,39 @@ double tmo_native_rate(const tmo_params *p, uint64_t n, uint32_t seed, uint64_t 
     free(h2);
     return dt > 0 ? (double)n / dt : 0.0;
 }
+
+/* ------------------------------------------------------ viewer colour map */
+/* cg_mc.c:38-67 (fragment shader FSHADER) restated in C: pixel (px, py) of a
+ * width x height target has gl_FragCoord = (px + 0.5, py + 0.5); uv = that /
+ * 800 (the shader divides by the literal 800, cg_mc.c:50); dr = |uv - 0.5|;
+ * shell = int(dr / 0.7071067811865476 * (shells - 1)) (truncation), clamped
+ * to the last shell for targets larger than 800; red = 2 / (1 + exp(-0.004
+ * heat)) - 1 (L = 2, b = 1, k = 0.004, cg_mc.c:58-62).  rgba8 is the usual
+ * UNORM conversion of (red, 0, 0, 1). */
+void tmo_colormap(const float *heats, uint32_t shells, uint32_t width, uint32_t height, float *red,
+                  unsigned char *rgba)
+{
+    const float mc = 0.7071067811865476f;
+    for (uint32_t py = 0; py < height; ++py) {
+        for (uint32_t px = 0; px < width; ++px) {
+            float ux = ((float)px + 0.5f) / 800.0f - 0.5f;
+            float uy = ((float)py + 0.5f) / 800.0f - 0.5f;
+            float dr = sqrtf(ux * ux + uy * uy);
+            int id = (int)((dr / mc) * (float)(shells - 1));
+            if (id > (int)shells - 1)
+                id = (int)shells - 1;
+            float heat = heats[id];
+            float fit = 2.0f / (1.0f + 1.0f * expf(-0.004f * heat)) - 1.0f;
+            size_t k = (size_t)py * width + px;
+            if (red)
+                red[k] = fit;
+            if (rgba) {
+                float c = fit < 0.0f ? 0.0f : (fit > 1.0f ? 1.0f : fit);
+                rgba[4 * k + 0] = (unsigned char)lrintf(c * 255.0f);
+                rgba[4 * k + 1] = 0;
+                rgba[4 * k + 2] = 0;
+                rgba[4 * k + 3] = 255;
+            }
+        }
+    }
+}

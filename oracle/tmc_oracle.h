@@ -111,6 +111,12 @@ int tmo_native_run(const tmo_params *p, uint64_t n, uint32_t seed, float *heat, 
  * replay over n photons (single thread, global rand). */
 double tmo_native_rate(const tmo_params *p, uint64_t n, uint32_t seed, uint64_t *steps);
 
+/* The viewer's fragment-shader colour map (cg_mc.c:38-67) on the CPU:
+ * red[height][width] float and rgba[height][width][4] (either may be NULL),
+ * row 0 = the bottom row (gl_FragCoord.y = 0.5). */
+void tmo_colormap(const float *heats, uint32_t shells, uint32_t width, uint32_t height, float *red,
+                  unsigned char *rgba);
+
 #ifdef __cplusplus
 }
 #endif

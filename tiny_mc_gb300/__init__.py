@@ -313,6 +313,44 @@ def format_report(heat: np.ndarray, heat2: np.ndarray, photons: int, p: Params) 
     return buf.value.decode()
 
 
+def _rep_setup(L) -> None:
+    if not getattr(L, "_rep_ready", False):
+        vp = ctypes.c_void_p
+        L.tmc_report_fp64.argtypes = [vp, ctypes.POINTER(Params), ctypes.c_uint64, vp, vp, vp]
+        L.tmc_report_fp64.restype = ctypes.c_int
+        L.tmc_format_report_fp64.argtypes = [ctypes.c_char_p, ctypes.c_size_t, vp, vp, ctypes.c_double,
+                                             ctypes.POINTER(Params)]
+        L.tmc_format_report_fp64.restype = ctypes.c_int
+        L._rep_ready = True
+
+
+def report_fp64(tally: np.ndarray, p: Params, photons: int):
+    """tiny_mc.c:60-66's numbers in FP64 on the GPU: (density, error, extra)."""
+    L = lib()
+    _rep_setup(L)
+    t = np.ascontiguousarray(tally, TALLY_DTYPE)
+    dens = np.zeros(p.shells - 1, np.float64)
+    err = np.zeros(p.shells - 1, np.float64)
+    extra = ctypes.c_double(0.0)
+    _check(L.tmc_report_fp64(t.ctypes.data, ctypes.byref(p), photons, dens.ctypes.data, err.ctypes.data,
+                             ctypes.byref(extra)), "tmc_report_fp64")
+    return dens, err, extra.value
+
+
+def format_report_fp64(density: np.ndarray, error: np.ndarray, extra: float, p: Params) -> str:
+    """The report table printed from FP64 values."""
+    L = lib()
+    _rep_setup(L)
+    d = np.ascontiguousarray(density, np.float64)
+    e = np.ascontiguousarray(error, np.float64)
+    n = L.tmc_format_report_fp64(None, 0, d.ctypes.data, e.ctypes.data, extra, ctypes.byref(p))
+    if n < 0:
+        _check(n, "tmc_format_report_fp64")
+    buf = ctypes.create_string_buffer(n + 1)
+    L.tmc_format_report_fp64(buf, n + 1, d.ctypes.data, e.ctypes.data, extra, ctypes.byref(p))
+    return buf.value.decode()
+
+
 def derived(p: Params):
     """(albedo, 1-albedo, shells_per_mfp) as float32, exactly as photon.c:8-9 computes them."""
     mu_a, mu_s = np.float32(p.mu_a), np.float32(p.mu_s)
@@ -324,6 +362,6 @@ def derived(p: Params):
 __all__ = [
     "Params", "params", "photon_batch", "photon_batch_fx", "photon_batch_device",
     "workspace_bytes", "set_plain_launch", "debug_rand", "tally_to_heat", "Batch", "BatchConfig",
-    "expected_steps", "photon_batch_static", "tally_sums", "format_report", "derived", "TmcError",
+    "expected_steps", "photon_batch_static", "report_fp64", "format_report_fp64", "tally_sums", "format_report", "derived", "TmcError",
     "MATH_EXACT", "MATH_FAST", "TALLY_DTYPE", "lib", "LIB_PATH",
 ]

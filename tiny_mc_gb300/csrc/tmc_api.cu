@@ -150,6 +150,37 @@ __global__ void tally_to_heat_kernel(const tmc_tally *t, uint32_t shells, double
     heat2[s] = (c * c) * sw2;
 }
 
+// tiny_mc.c:60-66 in FP64 from exact tallies: t = 4 pi MPS^3 N / 1e12 (cm^3),
+// density[i] = heat[i] / t / (i^2 + i + 1/3), error[i] = sqrt(heat2[i] -
+// heat[i]^2 / N) / t / (i^2 + i + 1/3) (NaN where the per-deposit variance
+// estimate goes negative, as the reference's does), extra = heat[S-1] / N.
+__global__ void report_fp64_kernel(const tmc_tally *t, uint32_t shells, double c, double mps,
+                                   double photons, double *density, double *error, double *extra)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= shells)
+        return;
+    const tmc_tally q = t[i];
+    const double heat = c * ((double)q.w_hi * 0x1p24 + (double)q.w_lo * 0x1p-40);
+    const double heat2 = (c * c) * ((double)q.w2_hi * 0x1p24 + (double)q.w2_lo * 0x1p-40);
+    const double vol = 4.0 * 3.14159265358979323846 * mps * mps * mps * photons / 1e12;
+    const double shell = (double)i * (double)i + (double)i + 1.0 / 3.0;
+    if (i + 1 < shells) {
+        density[i] = heat / vol / shell;
+        error[i] = sqrt(heat2 - heat * heat / photons) / vol / shell;
+    } else {
+        *extra = heat / photons;
+    }
+}
+
+cudaError_t launch_report_fp64(const tmc_tally *d_tally, uint32_t shells, double c, double mps,
+                               double photons, double *d_out, cudaStream_t stream)
+{
+    report_fp64_kernel<<<(shells + 255) / 256, 256, 0, stream>>>(d_tally, shells, c, mps, photons, d_out,
+                                                                  d_out + shells, d_out + 2 * shells);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_tally_to_heat(const tmc_tally *d_tally, uint32_t shells, double c,
                                  double *d_heat, double *d_heat2, cudaStream_t stream)
 {
@@ -344,6 +375,56 @@ int tmc_photon_batch_device(tmc_tally *d_tally, uint64_t n_photons, const tmc_pa
     if (e != cudaSuccess)
         return set_cuda_error(e, "walk_plain launch");
     return TMC_OK;
+}
+
+int tmc_report_fp64_device(const tmc_tally *d_tally, const tmc_params *p, uint64_t photons, double *d_out,
+                           void *stream)
+{
+    int st = validate(p);
+    if (st)
+        return st;
+    if (!d_tally || !d_out || photons == 0)
+        return TMC_E_INVALID;
+    const Derived d = derive(p->mu_a, p->mu_s, p->microns_per_shell, p->shells);
+    cudaError_t e = launch_report_fp64(d_tally, p->shells, (double)d.c, (double)p->microns_per_shell,
+                                       (double)photons, d_out, reinterpret_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? TMC_OK : set_cuda_error(e, "tmc_report_fp64_device");
+}
+
+int tmc_report_fp64(const tmc_tally *tally, const tmc_params *p, uint64_t photons, double *density,
+                    double *error, double *extra)
+{
+    int st = validate(p);
+    if (st)
+        return st;
+    if (!tally || !density || !error || !extra || photons == 0)
+        return TMC_E_INVALID;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    DeviceCtx *c = current_ctx(&st);
+    if (!c)
+        return st;
+    if ((st = ensure_buffers(*c, p->shells)))
+        return st;
+    const uint32_t S = p->shells;
+    double *d_out = nullptr;
+    cudaError_t e = cudaMallocAsync(&d_out, sizeof(double) * (2 * S + 1), c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->tally, tally, sizeof(tmc_tally) * S, cudaMemcpyHostToDevice, c->stream);
+    const Derived d = derive(p->mu_a, p->mu_s, p->microns_per_shell, S);
+    if (e == cudaSuccess)
+        e = launch_report_fp64(c->tally, S, (double)d.c, (double)p->microns_per_shell, (double)photons,
+                               d_out, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(density, d_out, sizeof(double) * (S - 1), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(error, d_out + S, sizeof(double) * (S - 1), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(extra, d_out + 2 * S, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (d_out)
+        cudaFreeAsync(d_out, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? TMC_OK : set_cuda_error(e, "tmc_report_fp64");
 }
 
 int tmc_tally_to_heat(const tmc_tally *tally, const tmc_params *p, double *heat, double *heat2)

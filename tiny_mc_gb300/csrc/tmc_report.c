@@ -62,3 +62,24 @@ int tmc_format_report(char *buf, size_t cap, const float *heat, const float *hea
         buf[cap - 1] = '\0';
     return o.len > 0x7fffffff ? TMC_E_OVERFLOW : (int)o.len;
 }
+
+/* The same table from FP64 values (tmc_report_fp64_device): radius column in
+ * float as tiny_mc.c:62 prints it, heat and error columns from the doubles. */
+int tmc_format_report_fp64(char *buf, size_t cap, const double *density, const double *error,
+                           double extra, const tmc_params *p)
+{
+    if (!density || !error || !p || p->shells == 0)
+        return TMC_E_INVALID;
+    if (buf && cap)
+        buf[0] = '\0';
+    out_t o = {buf, cap, 0};
+    put(&o, "# Radius\tHeat\n");
+    put(&o, "# [microns]\t[W/cm^3]\tError\n");
+    for (unsigned i = 0; i < p->shells - 1; ++i)
+        put(&o, "%6.0f\t%12.5f\t%12.5f\n", (double)((float)i * p->microns_per_shell), density[i],
+            error[i]);
+    put(&o, "# extra\t%12.5f\n", extra);
+    if (buf && cap && o.len >= cap)
+        buf[cap - 1] = '\0';
+    return o.len > 0x7fffffff ? TMC_E_OVERFLOW : (int)o.len;
+}

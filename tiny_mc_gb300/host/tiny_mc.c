@@ -6,7 +6,10 @@
  * tiny_mc.c:47-49 is ONE tmc_photon_batch() call on the GPU.
  *
  * Optional arguments override the macros at run time:
- *     tiny_mc [photons [seed [exact|fast]]]
+ *     tiny_mc [photons [seed [exact|fast [float|fp64 [image.ppm]]]]]
+ * "fp64" prints the table from the GPU's FP64 normalisation of the exact
+ * tallies instead of the float arrays; image.ppm writes the viewer's colour
+ * map of the heat array (cg_mc.c:38-67) as an 800x800 binary PPM.
  */
 #define _POSIX_C_SOURCE 199309L
 #include <stdio.h>
@@ -61,6 +64,8 @@ int main(int argc, char **argv)
         seed = strtoull(argv[2], NULL, 10);
     if (argc > 3 && strcmp(argv[3], "fast") == 0)
         p.math = TMC_MATH_FAST;
+    const int fp64 = argc > 4 && strcmp(argv[4], "fp64") == 0;
+    const char *ppm = argc > 5 ? argv[5] : NULL;
     p.seed = seed;
 
     printf("# %s\n# %s\n# %s\n", "Tiny Monte Carlo by Scott Prahl (http://omlc.ogi.edu)",
@@ -70,8 +75,10 @@ int main(int argc, char **argv)
     printf("# Absorption = %8.3f/cm\n", (double)p.mu_a);
     printf("# Photons    = %8llu\n#\n", photons);
 
+    static tmc_tally tally[SHELLS];
     double start = wall_seconds();
-    int st = tmc_photon_batch(heat, heat2, photons, &p);
+    int st = fp64 ? tmc_photon_batch_fx(tally, photons, &p, NULL)
+                  : tmc_photon_batch(heat, heat2, photons, &p);
     double end = wall_seconds();
     if (st != TMC_OK) {
         fprintf(stderr, "tmc_photon_batch: %s (%s)\n", tmc_strerror(st), tmc_last_error());
@@ -81,14 +88,42 @@ int main(int argc, char **argv)
     printf("# %lf seconds\n", elapsed);
     printf("# %lf K photons per second\n", 1e-3 * (double)photons / elapsed);
 
-    int need = tmc_format_report(NULL, 0, heat, heat2, photons, &p);
-    if (need < 0)
-        return 1;
-    char *buf = (char *)malloc((size_t)need + 1);
-    if (!buf)
-        return 1;
-    tmc_format_report(buf, (size_t)need + 1, heat, heat2, photons, &p);
+    int need;
+    char *buf;
+    if (fp64) {
+        static double density[SHELLS], error[SHELLS], h[SHELLS], h2[SHELLS];
+        double extra = 0.0;
+        if (tmc_report_fp64(tally, &p, photons, density, error, &extra) != TMC_OK)
+            return 1;
+        tmc_tally_to_heat(tally, &p, h, h2);
+        for (int i = 0; i < SHELLS; ++i) {
+            heat[i] = (float)h[i];
+            heat2[i] = (float)h2[i];
+        }
+        need = tmc_format_report_fp64(NULL, 0, density, error, extra, &p);
+        if (need < 0 || !(buf = (char *)malloc((size_t)need + 1)))
+            return 1;
+        tmc_format_report_fp64(buf, (size_t)need + 1, density, error, extra, &p);
+    } else {
+        need = tmc_format_report(NULL, 0, heat, heat2, photons, &p);
+        if (need < 0 || !(buf = (char *)malloc((size_t)need + 1)))
+            return 1;
+        tmc_format_report(buf, (size_t)need + 1, heat, heat2, photons, &p);
+    }
     fputs(buf, stdout);
     free(buf);
+    if (ppm) {
+        static unsigned char rgba[800 * 800 * 4];
+        if (tmc_colormap_host(heat, SHELLS, 800, 800, NULL, rgba) != TMC_OK)
+            return 1;
+        FILE *f = fopen(ppm, "wb");
+        if (!f)
+            return 1;
+        fprintf(f, "P6\n800 800\n255\n");
+        for (int y = 799; y >= 0; --y)          /* top row first; row 0 is the bottom */
+            for (int x = 0; x < 800; ++x)
+                fwrite(&rgba[4 * (y * 800 + x)], 1, 3, f);
+        fclose(f);
+    }
     return 0;
 }
