@@ -468,9 +468,10 @@ def run_serve(args):
     cap.  Three measurements on one server:
       1. calibration: the first requests of the trace submitted at once give
          the mean photon steps per request and the server's throughput, hence
-         the offered load of the configured rate (2000/s) against capacity;
-      2. the configured rate for a fixed window (no drain): throughput and
-         the latency of what completed while the queue grows;
+      2. the configured rate for a fixed window (no drain): the server is
+         saturated, so photon steps walked per second there is its capacity,
+         and 2000/s x mean steps per request / capacity is the offered load;
+         plus the latency of what completed while the queue grows;
       3. the same trace with arrivals slowed to 70 % of capacity: p50/p99
          latency of a stream the GPU can sustain."""
     import numpy as np
@@ -490,23 +491,25 @@ def run_serve(args):
     calib_steps = float(res_c["photon_steps"].sum())
     mean_steps = calib_steps / max(1, done_c)
     capacity = calib_steps / t_c
-    offered = 2000.0 * mean_steps / capacity
     # 2. configured rate, fixed window
     W = args.serve_window
     sel = slice(C, C + int(2000.0 * W * 1.2))
     a2 = arr[sel] - arr[sel][0]
     clocks = ClockSampler(None)
     clocks.start()
+    w0 = s.work()
     t0 = time.perf_counter()
     res_o, done_o = s.run_trace(req[sel], a2, time_limit_s=W)
     t_o = time.perf_counter() - t0
+    saturated = (s.work() - w0) / t_o          # the GPU never runs out of work here
+    offered = 2000.0 * mean_steps / saturated
     arrived = int(np.sum(a2 <= t_o))
     got = res_o["photons"] > 0
     lat_o = res_o["latency_s"][got]
     s.close()
     # 3. slowed to 70 % of capacity
     s = Server(slots=args.serve_slots, math=1 if args.math == "fast" else 0)
-    rate = 0.7 * capacity / mean_steps
+    rate = 0.7 * saturated / mean_steps
     n3 = max(50, min(int(rate * args.serve_duration), n_total - C))
     sel3 = slice(C, C + n3)
     a3 = (arr[sel3] - arr[sel3][0]) * (2000.0 / rate)
@@ -532,7 +535,8 @@ def run_serve(args):
         "requests": n3, "completed": int(done_s), "arrival_rate_per_s": rate,
         "reached_target_frac": float(np.mean(res_s["reached_target"][got3])) if got3.any() else None,
         "calibration": {"requests": C, "mean_photon_steps_per_request": mean_steps,
-                        "capacity_photon_steps_per_s": capacity,
+                        "calibration_photon_steps_per_s": capacity,
+                        "saturated_photon_steps_per_s": saturated,
                         "offered_load_at_2000_per_s": offered},
         "at_2000_per_s_window": {"window_s": W, "arrived": arrived, "completed": int(done_o),
                                  "photons_per_s": float(res_o["photons"].sum()) / t_o,

@@ -303,6 +303,8 @@ int tmc_server_poll(tmc_server *s, uint64_t request_id, int *done);
 /* Result of a finished request (then forgotten); tally [shells] may be NULL. */
 int tmc_server_result(tmc_server *s, uint64_t request_id, tmc_tally *tally, tmc_request_result *res);
 int tmc_server_stats(tmc_server *s, uint64_t *photons, uint64_t *photon_steps, uint64_t *waves);
+/* Photon steps walked so far, including those of requests still running. */
+int tmc_server_work(tmc_server *s, uint64_t *photon_steps);
 /* Replays an arrival trace in real time (arrival_s sorted, seconds from the
  * start): admits requests as they arrive and slots free up, drives the server
  * until all complete or time_limit_s (0 = none) passes.  results[i] is zero

@@ -1,6 +1,8 @@
 """The request server on the GPU: a request's result is the same alone and in
 a mix of concurrent requests, equals the plain kernel over the same photons,
 stops by its rule, and admission refuses requests when slots are full."""
+import math
+
 import numpy as np
 import pytest
 
@@ -94,3 +96,36 @@ def test_run_trace_small(tmc_mod):
     photons, steps, waves = s.stats()
     assert photons == int(res["photons"].sum()) and waves > 0
     s.close()
+
+
+def test_rse_from_exact_batch_probes_with_wraps(tmc_mod):
+    """One shell and albedo 0.9999 with 2048-photon batches: each batch's sum
+    of w in the probe shell (~2e7 weight units) exceeds 2^64 fixed-point
+    units, so the per-item probe must count its wraps.  The server's RSE must
+    equal, to the last bit, the batch-means RSE recomputed from per-batch
+    plain-kernel tallies of the same photons."""
+    from tiny_mc_gb300.serve import Server
+    r = req(mu_a=0.1, mu_s=1000.0, shells=1, rse=1e-9, cap=32 * 2048, base=77 << 32)
+    s = Server(slots=4, steps_per_batch=float(1 << 28))
+    rid = s.submit(r)
+    tally, res = s.run({rid: 1})[rid]
+    s.close()
+    B = int(res["batch_photons"])
+    assert B == 2048 and int(res["batches"]) == 32 and not res["reached_target"]
+    xs = []
+    for j in range(32):
+        p = tmc_mod.params(shells=1, microns_per_shell=50.0, mu_a=0.1, mu_s=1000.0, seed=1,
+                           photon_id_base=(77 << 32) + j * B, math="fast")
+        t, _ = tmc_mod.photon_batch_fx(B, p)
+        xs.append(float(int(t["w_hi"][0])) * 2.0 ** 24 + float(int(t["w_lo"][0])) * 2.0 ** -40)
+    assert max(xs) > 2.0 ** 24          # the per-batch sums did wrap 64 bits
+    k = len(xs)
+    tot = 0.0
+    for x in xs:          # in batch order, uncompensated, as the server sums
+        tot += x
+    m = tot / k
+    ss = 0.0
+    for x in xs:
+        ss += (x - m) * (x - m)
+    rse = math.sqrt(ss / (k - 1) / k) / m
+    assert res["rse"] == rse

@@ -36,13 +36,14 @@ template <int BLOCK, class M>
 __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
 {
     extern __shared__ __align__(16) uint32_t smem[];
-    __shared__ uint32_t sh_item, sh_next;
+    __shared__ uint32_t sh_item, sh_next, sh_probe_wraps;
     uint32_t *my = smem + 4 * a.max_shells + threadIdx.x;
 
     for (;;) {
         if (threadIdx.x == 0) {
             sh_item = (uint32_t)min(atomicAdd(a.item_counter, 1ull), 0xffffffffull);
             sh_next = 0;
+            sh_probe_wraps = 0;
         }
         __syncthreads();
         const uint32_t it = sh_item;
@@ -60,15 +61,17 @@ __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
         src.count = item.count;
         src.first = pr.id_base + item.first;
         unsigned long long *g = a.tally + 4 * pr.tally_offset;
-        const uint32_t steps = walk_loop<BLOCK, M>(pr.c, src, a.keys, smem, g, my);
+        const uint32_t ps = min(a.probe_shell, S - 1);
+        const uint32_t steps = walk_loop<BLOCK, M>(pr.c, src, a.keys, smem, g, my,
+                                                   a.item_probe ? &sh_probe_wraps : nullptr, ps);
 
         __syncthreads();
         flush_tally<BLOCK>(smem, S, g);
         if (a.item_probe && threadIdx.x == 0) {
-            // this item's own sum of w in the probe shell (its 64-bit shared
-            // sum cannot wrap: the planner bounds the item's total weight)
-            const uint32_t ps = min(a.probe_shell, S - 1);
-            a.item_probe[it] = ((unsigned long long)smem[S + ps] << 32) | smem[ps];
+            // this item's own sum of w in the probe shell, 128-bit: the
+            // block's 64-bit shared sum plus its counted 2^64 wraps
+            a.item_probe[2 * (size_t)it] = ((unsigned long long)smem[S + ps] << 32) | smem[ps];
+            a.item_probe[2 * (size_t)it + 1] = sh_probe_wraps;
         }
         const unsigned long long tot = warp_sum_u64(steps);
         if ((threadIdx.x & 31u) == 0 && tot)

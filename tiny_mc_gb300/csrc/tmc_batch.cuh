@@ -33,7 +33,7 @@ struct BatchArgs {
     unsigned long long *tally;         // [total shells][4]
     unsigned long long *steps;         // [problems]
     unsigned long long *item_counter;  // zero at launch
-    unsigned long long *item_probe;    // [n_items] or null
+    unsigned long long *item_probe;    // [n_items][2] (128-bit, lo then hi) or null
 };
 
 size_t walk_batch_smem(uint32_t max_shells, int block);

@@ -183,14 +183,19 @@ __device__ __forceinline__ void fx40_split(float w, uint32_t &lo, uint32_t &hi)
 // high word, and a wrap of the high word carries 2^64 units into the 128-bit
 // global tally.  The global word receives only such carries until the final
 // flush, so no epoch barriers are needed however many photons a block walks.
+// wraps (may be null) additionally counts this tally's 2^64 wraps.
 __device__ __forceinline__ void tally_add(uint32_t *sh_lo, uint32_t *sh_hi,
-                                          unsigned long long *g_hi, uint32_t lo, uint32_t hi)
+                                          unsigned long long *g_hi, uint32_t lo, uint32_t hi,
+                                          uint32_t *wraps = nullptr)
 {
     const uint32_t old = atomicAdd(sh_lo, lo);
     hi += (old + lo < old) ? 1u : 0u;
     const uint32_t oh = atomicAdd(sh_hi, hi);
-    if (oh + hi < oh)
+    if (oh + hi < oh) {
         atomicAdd(g_hi, 1ull);
+        if (wraps)
+            atomicAdd(wraps, 1u);
+    }
 }
 
 // Flush a 64-bit partial sum into a 128-bit global tally.

@@ -9,11 +9,10 @@
 //    max_shells x 32 bytes) or refuses it with TMC_E_BUSY, so the caller
 //    queues; the tally and RNG state never leave the device while it runs;
 //  * walks a request in RSE batches of B photons (B a power of two chosen so
-//    one batch is about `steps_per_batch` photon steps, at least one photon
-//    per thread of a block).  A batch is one or more work items of the
-//    batched kernel, each walked by one block, which also writes the item's
-//    own sum of w in the probe shell; items are small enough that that 64-bit
-//    shared sum cannot wrap;
+//    one batch is about `steps_per_batch` photon steps, at least four photons
+//    per thread of a block).  A batch is one work item of the batched kernel,
+//    walked by one block, which also writes the item's own 128-bit sum of w
+//    in the probe shell;
 //  * stops a request only at fixed batch counts (min_batches, then doubling):
 //    there it computes the batch-means RSE of the probe shell in FP64 over
 //    batches 0..k-1 in order, and stops if RSE <= target or the cap is
@@ -63,7 +62,8 @@ struct Req {
     uint64_t max_batches = 0;
     uint64_t issued = 0, done = 0;  // work items
     uint64_t next_decision = 0;     // in batches
-    std::vector<unsigned long long> probe;   // per item: sum of w in the probe shell (2^-40 units)
+    std::vector<unsigned long long> probe;   // per item: 128-bit sum of w in the probe shell
+                                             // (2^-40 units), lo and hi
     double t_submit = 0.0;
 };
 
@@ -135,27 +135,15 @@ void destroy_server(tmc_server *s)
 }
 
 // Photons per RSE batch: a power of two near steps_per_batch / E[steps], in
-// [block, 8192] (at least one photon per thread of the block walking it).
+// [4 x block, 65536]: at least four photons per thread of the block walking
+// it, so lanes that finish early are few.
 uint32_t batch_photons(const tmc_server_config &cfg, double est_steps)
 {
     const double want = cfg.steps_per_batch / std::max(1.0, est_steps);
-    uint32_t b = cfg.block;
-    while (b < 8192 && 2.0 * b <= want)
+    uint32_t b = 4 * cfg.block;
+    while (b < 65536 && 2.0 * b <= want)
         b *= 2;
     return b;
-}
-
-// Photons per work item: the batch, halved until the item is at most
-// 2^24 (1 - albedo) photons.  A photon deposits at most 1/(1-albedo) weight
-// units, so an item's sum in one shell stays below 2^64 fixed-point units and
-// its 64-bit shared sum cannot wrap.
-uint32_t item_photons(uint32_t batch, const Derived &d)
-{
-    const double bound = std::floor(16777216.0 * (1.0 - (double)d.albedo));
-    uint32_t p = batch;
-    while (p > 1 && (double)p > bound)
-        p /= 2;
-    return p;
 }
 
 double expected_steps_host(float albedo)
@@ -180,8 +168,10 @@ double batch_rse(const std::vector<unsigned long long> &probe, uint32_t ipb, uin
 {
     std::vector<double> x(k, 0.0);
     for (uint64_t j = 0; j < k; ++j)
-        for (uint32_t i = 0; i < ipb; ++i)
-            x[j] += (double)probe[j * ipb + i] * 0x1p-40;
+        for (uint32_t i = 0; i < ipb; ++i) {
+            const uint64_t g = j * ipb + i;
+            x[j] += (double)probe[2 * g + 1] * 0x1p24 + (double)probe[2 * g] * 0x1p-40;
+        }
     double sum = 0.0;
     for (uint64_t j = 0; j < k; ++j)
         sum += x[j];
@@ -252,7 +242,9 @@ int harvest(tmc_server *s, Wave &w)
         const BatchItemDev &it = w.h_items[i];
         const uint64_t id = s->slot_req[it.problem];
         Req &q = s->active[id];
-        q.probe[it.first / q.item_photons] = w.h_probe[i];
+        const uint64_t g = it.first / q.item_photons;
+        q.probe[2 * g] = w.h_probe[2 * (size_t)i];
+        q.probe[2 * g + 1] = w.h_probe[2 * (size_t)i + 1];
         ++q.done;
         if (touched.empty() || touched.back() != id)
             touched.push_back(id);
@@ -298,8 +290,8 @@ int launch_wave(tmc_server *s, Wave &w)
             it.first = (q.issued + j) * (uint64_t)q.item_photons;
         }
         q.issued += k;
-        if (q.probe.size() < q.issued)
-            q.probe.resize(q.issued, 0ull);
+        if (q.probe.size() < 2 * q.issued)
+            q.probe.resize(2 * q.issued, 0ull);
     }
     s->rr = m ? (s->rr + 1) % m : 0;
     if (n == 0)
@@ -325,8 +317,8 @@ int launch_wave(tmc_server *s, Wave &w)
                               w.stream);
     }
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(w.h_probe, w.d_probe, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost,
-                            w.stream);
+        e = cudaMemcpyAsync(w.h_probe, w.d_probe, 2 * sizeof(unsigned long long) * n,
+                            cudaMemcpyDeviceToHost, w.stream);
     if (e == cudaSuccess)
         e = cudaEventRecord(w.done, w.stream);
     if (e != cudaSuccess)
@@ -377,7 +369,7 @@ void tmc_server_config_default(tmc_server_config *c)
     c->math = TMC_MATH_FAST;
     c->block = 128;
     c->max_items_per_request = 1024;
-    c->steps_per_batch = 2097152.0;
+    c->steps_per_batch = 8388608.0;
 }
 
 int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
@@ -426,13 +418,13 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
         if (e == cudaSuccess)
             e = cudaMalloc(&w.d_items, sizeof(BatchItemDev) * s->items_cap);
         if (e == cudaSuccess)
-            e = cudaMalloc(&w.d_probe, sizeof(unsigned long long) * s->items_cap);
+            e = cudaMalloc(&w.d_probe, 2 * sizeof(unsigned long long) * s->items_cap);
         if (e == cudaSuccess)
             e = cudaMalloc(&w.d_counter, sizeof(unsigned long long));
         if (e == cudaSuccess)
             e = cudaMallocHost(&w.h_items, sizeof(BatchItemDev) * s->items_cap);
         if (e == cudaSuccess)
-            e = cudaMallocHost(&w.h_probe, sizeof(unsigned long long) * s->items_cap);
+            e = cudaMallocHost(&w.h_probe, 2 * sizeof(unsigned long long) * s->items_cap);
     }
     if (e != cudaSuccess)
         return set_cuda_error(e, "tmc_server_create");
@@ -466,8 +458,8 @@ int tmc_server_submit(tmc_server *s, const tmc_request *r, uint64_t *id)
     q.r = *r;
     q.d = derive(r->mu_a, r->mu_s, r->microns_per_shell, r->shells);
     q.batch = batch_photons(s->cfg, expected_steps_host(q.d.albedo));
-    q.item_photons = item_photons(q.batch, q.d);
-    q.items_per_batch = q.batch / q.item_photons;
+    q.item_photons = q.batch;
+    q.items_per_batch = 1;
     q.max_batches = std::max<uint64_t>(1, (r->max_photons + q.batch - 1) / q.batch);
     q.next_decision = std::min<uint64_t>(s->cfg.min_batches, q.max_batches);
     q.slot = s->free_slots.back();
@@ -558,6 +550,27 @@ int tmc_server_stats(tmc_server *s, uint64_t *photons, uint64_t *photon_steps, u
         *photon_steps = s->steps;
     if (waves)
         *waves = s->n_waves;
+    return TMC_OK;
+}
+
+int tmc_server_work(tmc_server *s, uint64_t *photon_steps)
+{
+    if (!s || !photon_steps)
+        return TMC_E_INVALID;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    // finished requests plus the device counters of the running ones (a wave
+    // adds to them as its blocks finish items)
+    std::vector<unsigned long long> cur(s->cfg.slots, 0);
+    cudaError_t e = cudaMemcpyAsync(cur.data(), s->d_steps, sizeof(unsigned long long) * s->cfg.slots,
+                                    cudaMemcpyDeviceToHost, s->admin);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s->admin);
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "tmc_server_work");
+    uint64_t t = s->steps;
+    for (const auto &kv : s->active)
+        t += cur[kv.second.slot];
+    *photon_steps = t;
     return TMC_OK;
 }
 

@@ -140,11 +140,14 @@ struct SharedSource {
 // died.  Warp-collective: all 32 lanes of every warp call it.  tally: the
 // block's shared histogram, 4 * shells words (low and high of sum w, then of
 // sum w^2); g: the problem's global 128-bit tally [shells][4] (receives only
-// carries here).  Returns this thread's photon steps.
+// carries here).  probe_wraps (may be null): counts the 2^64 wraps of the
+// block's sum of w in shell probe_shell.  Returns this thread's photon steps.
 template <int BLOCK, class M, class Source>
 __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
                                               const PhiloxKeys &keys, uint32_t *tally,
-                                              unsigned long long *g, uint32_t *my)
+                                              unsigned long long *g, uint32_t *my,
+                                              uint32_t *probe_wraps = nullptr,
+                                              uint32_t probe_shell = 0)
 {
     const uint32_t S = c.shells;
     const unsigned lane = threadIdx.x & 31u;
@@ -225,7 +228,8 @@ __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
                 uint32_t *t0 = tally + shell;
                 uint32_t lo, hi;
                 fx40_split(weight, lo, hi);
-                tally_add(t0, t0 + S, &g[4 * shell + 1], lo, hi);
+                tally_add(t0, t0 + S, &g[4 * shell + 1], lo, hi,
+                          shell == probe_shell ? probe_wraps : nullptr);
                 fx40_split(__fmul_rn(weight, weight), lo, hi);
                 tally_add(t0 + 2 * S, t0 + 3 * S, &g[4 * shell + 3], lo, hi);
                 weight = M::mul(weight, c.albedo);

@@ -66,6 +66,8 @@ def _setup(L):
     L.tmc_server_result.restype = i32
     L.tmc_server_stats.argtypes = [vp, vp, vp, vp]
     L.tmc_server_stats.restype = i32
+    L.tmc_server_work.argtypes = [vp, ctypes.POINTER(u64)]
+    L.tmc_server_work.restype = i32
     L.tmc_server_run_trace.argtypes = [vp, vp, vp, ctypes.c_uint32, ctypes.c_double, vp, vp]
     L.tmc_server_run_trace.restype = i32
     L.tmc_server_destroy.argtypes = [vp]
@@ -152,6 +154,12 @@ class Server:
         _check(lib().tmc_server_stats(self.handle, ctypes.byref(p), ctypes.byref(s), ctypes.byref(w)),
                "tmc_server_stats")
         return p.value, s.value, w.value
+
+    def work(self) -> int:
+        """Photon steps walked so far, running requests included."""
+        w = ctypes.c_uint64(0)
+        _check(lib().tmc_server_work(self.handle, ctypes.byref(w)), "tmc_server_work")
+        return w.value
 
     def close(self):
         if getattr(self, "handle", None):
