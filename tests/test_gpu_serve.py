@@ -66,9 +66,9 @@ def test_result_equals_plain_kernel_and_rule(tmc_mod):
             assert res["rse"] <= r["target_rse"]
         else:
             assert n >= int(r["max_photons"]) or b * int(res["batch_photons"]) >= int(r["max_photons"])
-        # decisions only at 32, 64, 128, ... batches, or at the cap
+        # decisions only at 16, 32, 64, ... batches, or at the cap
         cap_b = -(-int(r["max_photons"]) // int(res["batch_photons"]))
-        assert b == cap_b or (b >= 32 and (b & (b - 1)) == 0)
+        assert b == cap_b or (b >= 16 and (b & (b - 1)) == 0)
 
 
 def test_admission_refuses_when_full(tmc_mod):

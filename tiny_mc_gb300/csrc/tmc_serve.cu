@@ -9,7 +9,7 @@
 //    max_shells x 32 bytes) or refuses it with TMC_E_BUSY, so the caller
 //    queues; the tally and RNG state never leave the device while it runs;
 //  * walks a request in RSE batches of B photons (B a power of two chosen so
-//    one batch is about `steps_per_batch` photon steps, at least four photons
+//    one batch is about `steps_per_batch` photon steps, at least two photons
 //    per thread of a block).  A batch is one work item of the batched kernel,
 //    walked by one block, which also writes the item's own 128-bit sum of w
 //    in the probe shell;
@@ -20,7 +20,9 @@
 //    request's result is the same alone and in any mix;
 //  * runs work in waves: launches of the batched kernel over a bounded
 //    number of pending items, taken round-robin from the active requests,
-//    with up to four waves in flight on four streams.  Requests that arrive
+//    with up to sixteen waves in flight on sixteen streams (a wave finishes
+//    with its slowest item, so many in flight keep the SMs fed past the
+//    stragglers).  Requests that arrive
 //    while waves run are admitted and their items join the next wave while
 //    earlier ones are still on the device; a request's items may be spread
 //    over several waves, and its stop decision waits until every item before
@@ -43,7 +45,7 @@ using namespace tmc;
 
 namespace {
 
-constexpr int WAVES = 4;
+constexpr int WAVES = 16;
 using Clock = std::chrono::steady_clock;
 
 double now_s()
@@ -135,12 +137,11 @@ void destroy_server(tmc_server *s)
 }
 
 // Photons per RSE batch: a power of two near steps_per_batch / E[steps], in
-// [4 x block, 65536]: at least four photons per thread of the block walking
-// it, so lanes that finish early are few.
+// [2 x block, 65536]: at least two photons per thread of the block walking it.
 uint32_t batch_photons(const tmc_server_config &cfg, double est_steps)
 {
     const double want = cfg.steps_per_batch / std::max(1.0, est_steps);
-    uint32_t b = 4 * cfg.block;
+    uint32_t b = 2 * cfg.block;
     while (b < 65536 && 2.0 * b <= want)
         b *= 2;
     return b;
@@ -364,7 +365,7 @@ void tmc_server_config_default(tmc_server_config *c)
     c->slots = 1024;
     c->max_shells = 501;
     c->probe_shell = 10;
-    c->min_batches = 32;
+    c->min_batches = 16;
     c->seed = 1;
     c->math = TMC_MATH_FAST;
     c->block = 128;
