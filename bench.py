@@ -56,6 +56,11 @@ def parse():
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--optics", choices=["cfg1", "cfg2"], default="cfg1",
+                    help="plain workload optics: cfg1 = params.h (101 shells, 50 um, MU_A 2, MU_S 20); "
+                         "cfg2 = high albedo (1001 shells, 10 um, MU_A 0.1, MU_S 100)")
+    ap.add_argument("--sweep-mu-a-min", type=float, default=0.01,
+                    help="sweep workload: lower end of the mu_a range (0.01 = config 3)")
     ap.add_argument("--workload", choices=["plain", "sweep", "serve"], default="plain",
                     help="plain: config 1 (default); sweep: the 4096-problem batched sweep; "
                          "serve: the request stream")
@@ -71,11 +76,19 @@ def parse():
     return ap.parse_args()
 
 
+OPTICS = {"cfg1": dict(shells=101, microns_per_shell=50.0, mu_a=2.0, mu_s=20.0),
+          "cfg2": dict(shells=1001, microns_per_shell=10.0, mu_a=0.1, mu_s=100.0)}
+
+
 def workload_config(args, world):
+    o = OPTICS[args.optics]
+    name = ("plain walk, 2^30 photons per GPU (config 1)" if args.optics == "cfg1" and
+            args.photons == 1 << 30 else f"plain walk, {args.photons} photons per GPU ({args.optics} optics)")
     return {
-        "workload": "plain walk, 2^30 photons per GPU (config 1)",
+        "workload": name,
         "photons_per_step_per_gpu": args.photons,
-        "shells": 101, "microns_per_shell": 50, "mu_a_per_cm": 2.0, "mu_s_per_cm": 20.0,
+        "shells": o["shells"], "microns_per_shell": o["microns_per_shell"], "mu_a_per_cm": o["mu_a"],
+        "mu_s_per_cm": o["mu_s"],
         "rng": "Philox-4x32-10 keyed by photon id, seed 1",
         "math": args.math,
         "tallies": "u64 shared / u128 global fixed point (2^-40)",
@@ -265,8 +278,9 @@ def run_ours(args):
     uuid = getattr(props, "uuid", None)
     device_id = f"GPU-{uuid}" if uuid is not None else None
 
-    S = 101
-    p = tmc.params(seed=1, photon_id_base=rank * args.photons, math=args.math)
+    optics = OPTICS[args.optics]
+    S = optics["shells"]
+    p = tmc.params(seed=1, photon_id_base=rank * args.photons, math=args.math, **optics)
     tmc.set_plain_launch(args.block, args.blocks_per_sm, 0)
     tally = torch.zeros((S, 4), dtype=torch.int64, device=dev)
     steps_ctr = torch.zeros(1, dtype=torch.int64, device=dev)
@@ -325,8 +339,8 @@ def run_ours(args):
     roofline = {
         "bound": "sfu", "achieved": achieved / 1e9, "peak": sfu_peak / 1e9, "unit": "Gop/s",
         "frac": achieved / sfu_peak,
-        "traffic": WALK_DRAM_BYTES_PER_LAUNCH,
-        "traffic_note": "DRAM bytes per launch (ncu); tally flush only, independent of photons",
+        "traffic": WALK_DRAM_BYTES_PER_LAUNCH if args.optics == "cfg1" else None,
+        "traffic_note": "DRAM bytes per launch (ncu, 101 shells); tally flush only, independent of photons",
         "algorithmic_unit": "4 SFU-class ops (log, sqrt, divide, sqrt) per photon step",
         "photon_steps_per_launch": photon_steps / args.steps,
         "peak_source": "measured live: MUFU lg2/sqrt/rcp probe (tmc_probe_sfu_rate)",
@@ -335,7 +349,7 @@ def run_ours(args):
     # the exact (bit-reproducible) arithmetic on the same workload, for reference
     value_exact = None
     if args.math == "fast" and not args.no_e2e:
-        pe = tmc.params(seed=1, photon_id_base=rank * args.photons, math="exact")
+        pe = tmc.params(seed=1, photon_id_base=rank * args.photons, math="exact", **optics)
         tmc.photon_batch_device(tally.data_ptr(), args.photons, pe, 0, ws.data_ptr(), sp)
         torch.cuda.synchronize()
         ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -396,7 +410,8 @@ def run_sweep(args):
     from tiny_mc_gb300.sweep import make_sweep
 
     torch.cuda.set_device(0)
-    sw = make_sweep(4096, seed=0, photon_scale=args.sweep_scale, min_photons=16)
+    sw = make_sweep(4096, seed=0, photon_scale=args.sweep_scale, min_photons=16,
+                    mu_a_range=(args.sweep_mu_a_min, 10.0))
     photons = int(sw["n_photons"].sum())
     b = tmc.Batch(sw, seed=1, math=args.math)
     t0 = time.perf_counter()

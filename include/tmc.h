@@ -220,6 +220,8 @@ typedef struct tmc_batch_config {
     int block;            /* threads per block: 128, 256 or 512 (0 = 256) */
     int items_per_block;  /* work items per resident block: load-balance granularity (0 = 8) */
     int use_graph;        /* 1: run through a captured CUDA graph, replayed on later runs */
+    int stream;           /* 1: two items open per block, lanes flow into the next item
+                             instead of waiting at a barrier for the slowest lane */
 } tmc_batch_config;
 
 int tmc_batch_create(tmc_batch **out, const tmc_problem *problems, uint32_t n_problems,
@@ -286,7 +288,7 @@ typedef struct tmc_server_config {
     uint32_t math;
     uint32_t block;                 /* 128, 256 or 512 */
     uint32_t max_items_per_request; /* RSE batches of one request in one wave */
-    uint32_t reserved;
+    uint32_t stream;                /* 1: barrier-free kernel (two items open per block) */
     double steps_per_batch;         /* target photon steps per RSE batch */
 } tmc_server_config;
 

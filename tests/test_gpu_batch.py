@@ -27,10 +27,12 @@ def plain_tally(tmc, prob, seed, math):
     return as_array(t), steps
 
 
-@pytest.mark.parametrize("math", ["exact", "fast"])
-def test_batch_equals_plain_per_problem(tmc_mod, math):
+@pytest.mark.parametrize("math,stream", [("exact", False), ("fast", False), ("exact", True),
+                                         ("fast", True)])
+def test_batch_equals_plain_per_problem(tmc_mod, math, stream):
     sw = small_sweep()
     b = tmc_mod.Batch(sw, seed=7, math=math)
+    b.set_config(256, 8, False, stream)
     b.run()
     tallies, steps = b.read()
     for i in range(len(sw)):
@@ -55,19 +57,42 @@ def test_batch_equals_oracle(tmc_mod, oracle_mod):
     b.close()
 
 
-@pytest.mark.parametrize("block,ipb,graph", [(128, 1, False), (256, 64, False), (512, 8, True),
-                                             (256, 8, True)])
-def test_batch_config_invariance(tmc_mod, block, ipb, graph):
+@pytest.mark.parametrize("block,ipb,graph,stream", [
+    (128, 1, False, False), (256, 64, False, False), (512, 8, True, False), (256, 8, True, False),
+    (128, 1, False, True), (256, 64, True, True), (512, 16, False, True), (128, 8, True, True)])
+def test_batch_config_invariance(tmc_mod, block, ipb, graph, stream):
     sw = small_sweep(n=30, seed=8)
     b = tmc_mod.Batch(sw, seed=2, math="fast")
     b.run()
     ref, ref_steps = b.read()
-    b.set_config(block, ipb, graph)
+    b.set_config(block, ipb, graph, stream)
     for _ in range(2):                 # second pass replays the graph
         b.run()
         t, s = b.read()
         assert np.array_equal(t, ref) and np.array_equal(s, ref_steps)
-    assert b.config() == {"block": block, "items_per_block": ipb, "use_graph": graph}
+    assert b.config() == {"block": block, "items_per_block": ipb, "use_graph": graph, "stream": stream}
+    b.close()
+
+
+def test_stream_kernel_heavy_tail_items(tmc_mod):
+    """High-albedo problems split into many small items (the case the
+    barrier-free kernel is for): tallies still equal the plain kernel's."""
+    from tiny_mc_gb300.sweep import PROBLEM_DTYPE
+    pr = np.zeros(6, PROBLEM_DTYPE)
+    pr["shells"] = [101, 501, 1, 101, 501, 7]
+    pr["microns_per_shell"] = 50.0
+    pr["mu_a"] = [0.1, 1.0, 0.05, 2.0, 0.2, 5.0]
+    pr["mu_s"] = [100.0, 200.0, 100.0, 20.0, 300.0, 1.0]
+    pr["n_photons"] = [3000, 2000, 1500, 50000, 1000, 20000]
+    pr["photon_id_base"] = np.concatenate([[0], np.cumsum(pr["n_photons"][:-1])])
+    b = tmc_mod.Batch(pr, seed=5, math="fast")
+    b.set_config(128, 64, False, True)
+    b.run()
+    t, s = b.read()
+    for i in range(len(pr)):
+        ref, steps = plain_tally(tmc_mod, pr[i], 5, "fast")
+        assert np.array_equal(as_array(b.tally_of(t, i)), ref), i
+        assert int(s[i]) == steps
     b.close()
 
 

@@ -24,14 +24,15 @@ MIX = [req(2.0, 20.0, 101, 0.02, base=1 << 32), req(0.5, 50.0, 501, 0.03, base=2
        req(0.02, 2.0, 101, 0.04, cap=1 << 16, base=5 << 32)]
 
 
-def test_alone_equals_in_mix(tmc_mod):
+@pytest.mark.parametrize("stream", [0, 1])
+def test_alone_equals_in_mix(tmc_mod, stream):
     from tiny_mc_gb300.serve import Server
     probe = req(1.0, 30.0, 101, 0.02, base=9 << 32)
-    s = Server(slots=8)
+    s = Server(slots=8, stream=1 - stream)      # alone on the other kernel
     rid = s.submit(probe)
     alone = s.run({rid: 101})[rid]
     s.close()
-    s = Server(slots=8)
+    s = Server(slots=8, stream=stream)
     ids = {s.submit(r): int(r["shells"]) for r in MIX[:3]}
     rid = s.submit(probe)
     ids[rid] = 101
@@ -46,9 +47,10 @@ def test_alone_equals_in_mix(tmc_mod):
     assert r_alone["rse"] == r_mix["rse"]
 
 
-def test_result_equals_plain_kernel_and_rule(tmc_mod):
+@pytest.mark.parametrize("stream", [0, 1])
+def test_result_equals_plain_kernel_and_rule(tmc_mod, stream):
     from tiny_mc_gb300.serve import Server
-    s = Server(slots=8)
+    s = Server(slots=8, stream=stream)
     ids = {s.submit(r): int(r["shells"]) for r in MIX}
     out = s.run(ids)
     s.close()
@@ -98,7 +100,8 @@ def test_run_trace_small(tmc_mod):
     s.close()
 
 
-def test_rse_from_exact_batch_probes_with_wraps(tmc_mod):
+@pytest.mark.parametrize("stream", [0, 1])
+def test_rse_from_exact_batch_probes_with_wraps(tmc_mod, stream):
     """One shell and albedo 0.9999 with 2048-photon batches: each batch's sum
     of w in the probe shell (~2e7 weight units) exceeds 2^64 fixed-point
     units, so the per-item probe must count its wraps.  The server's RSE must
@@ -106,7 +109,7 @@ def test_rse_from_exact_batch_probes_with_wraps(tmc_mod):
     plain-kernel tallies of the same photons."""
     from tiny_mc_gb300.serve import Server
     r = req(mu_a=0.1, mu_s=1000.0, shells=1, rse=1e-9, cap=32 * 2048, base=77 << 32)
-    s = Server(slots=4, steps_per_batch=float(1 << 28))
+    s = Server(slots=4, steps_per_batch=float(1 << 28), stream=stream)
     rid = s.submit(r)
     tally, res = s.run({rid: 1})[rid]
     s.close()

@@ -59,7 +59,7 @@ class Params(ctypes.Structure):
 class BatchConfig(ctypes.Structure):
     """``tmc_batch_config``."""
     _fields_ = [("block", ctypes.c_int), ("items_per_block", ctypes.c_int),
-                ("use_graph", ctypes.c_int)]
+                ("use_graph", ctypes.c_int), ("stream", ctypes.c_int)]
 
 
 TALLY_DTYPE = np.dtype([("w_lo", "<u8"), ("w_hi", "<u8"), ("w2_lo", "<u8"), ("w2_hi", "<u8")])
@@ -236,14 +236,16 @@ class Batch:
         self.offsets = np.zeros(len(self.problems) + 1, np.uint64)
         _check(lib().tmc_batch_tally_offsets(h, self.offsets.ctypes.data), "tmc_batch_tally_offsets")
 
-    def set_config(self, block: int = 0, items_per_block: int = 0, use_graph: bool = False) -> None:
-        c = BatchConfig(block, items_per_block, int(use_graph))
+    def set_config(self, block: int = 0, items_per_block: int = 0, use_graph: bool = False,
+                   stream: bool = False) -> None:
+        c = BatchConfig(block, items_per_block, int(use_graph), int(stream))
         _check(lib().tmc_batch_set_config(self.handle, ctypes.byref(c)), "tmc_batch_set_config")
 
     def config(self) -> dict:
         c = BatchConfig()
         _check(lib().tmc_batch_get_config(self.handle, ctypes.byref(c)), "tmc_batch_get_config")
-        return {"block": c.block, "items_per_block": c.items_per_block, "use_graph": bool(c.use_graph)}
+        return {"block": c.block, "items_per_block": c.items_per_block, "use_graph": bool(c.use_graph),
+                "stream": bool(c.stream)}
 
     def autotune(self, scale: float = 1.0 / 64, max_steps_per_photon: float = 2e4) -> float:
         ms = ctypes.c_double(0.0)

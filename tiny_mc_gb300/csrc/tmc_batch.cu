@@ -176,7 +176,7 @@ struct tmc_batch {
     uint64_t seed = 0;
     uint32_t math = TMC_MATH_EXACT;
     uint32_t max_shells = 0;
-    tmc_batch_config cfg{256, 8, 0};
+    tmc_batch_config cfg{256, 8, 0, 0};
     int device = -1;
     int sms = 0;
     int grid = 0;            // resident blocks for the current config (set by plan)
@@ -198,11 +198,15 @@ struct tmc_batch {
 
 namespace {
 
-size_t batch_smem(const tmc_batch *b, int block) { return walk_batch_smem(b->max_shells, block); }
+size_t batch_smem(const tmc_batch *b, int block)
+{
+    return b->cfg.stream ? walk_stream_smem(b->max_shells, block) : walk_batch_smem(b->max_shells, block);
+}
 
 cudaError_t grid_for(const tmc_batch *b, int *grid)
 {
-    return walk_batch_prepare(b->cfg.block, b->math, b->max_shells, b->sms, grid);
+    return b->cfg.stream ? walk_stream_prepare(b->cfg.block, b->math, b->max_shells, b->sms, grid)
+                         : walk_batch_prepare(b->cfg.block, b->math, b->max_shells, b->sms, grid);
 }
 
 // Split problems into items of about equal estimated photon steps.
@@ -274,8 +278,8 @@ cudaError_t enqueue(const tmc_batch *b, cudaStream_t s)
     cudaError_t e = cudaMemsetAsync(b->d_tally, 0, sizeof(tmc_tally) * b->offsets[n], s);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(b->d_steps, 0, sizeof(unsigned long long) * std::max<size_t>(1, n), s);
-    if (e == cudaSuccess)
-        e = cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess)   // item counter and error flag
+        e = cudaMemsetAsync(b->d_counter, 0, 2 * sizeof(unsigned long long), s);
     if (e != cudaSuccess || b->n_items == 0)
         return e;
     // launch only (no attribute calls, so it can be captured): plan() has set
@@ -291,6 +295,12 @@ cudaError_t enqueue(const tmc_batch *b, cudaStream_t s)
     a.steps = b->d_steps;
     a.item_counter = b->d_counter;
     a.item_probe = nullptr;
+    a.error = reinterpret_cast<unsigned *>(b->d_counter + 1);
+    if (b->cfg.stream) {
+        // two items open per block: no more blocks than half the items
+        const int grid = std::max(1, std::min<int>(b->grid, (int)((b->n_items + 1) / 2)));
+        return walk_stream_launch(a, b->cfg.block, b->math, grid, s);
+    }
     const int grid = std::max(1, std::min<int>(b->grid, (int)b->n_items));
     return walk_batch_launch(a, b->cfg.block, b->math, grid, s);
 }
@@ -441,7 +451,7 @@ int tmc_batch_create(tmc_batch **out, const tmc_problem *problems, uint32_t n_pr
     if (e == cudaSuccess)
         e = cudaMalloc(&b->d_steps, sizeof(unsigned long long) * std::max<size_t>(1, n_problems));
     if (e == cudaSuccess)
-        e = cudaMalloc(&b->d_counter, sizeof(unsigned long long));
+        e = cudaMalloc(&b->d_counter, 2 * sizeof(unsigned long long));
     if (e != cudaSuccess) {
         int r = set_cuda_error(e, "tmc_batch_create");
         free_batch(b.release());
@@ -460,10 +470,12 @@ int tmc_batch_set_config(tmc_batch *b, const tmc_batch_config *cfg)
         return TMC_E_INVALID;
     if (cfg->items_per_block < 0 || cfg->items_per_block > 1024)
         return TMC_E_INVALID;
-    if (batch_smem(b, block) > b->smem_optin)
+    const size_t need = cfg->stream ? walk_stream_smem(b->max_shells, block)
+                                    : walk_batch_smem(b->max_shells, block);
+    if (need > b->smem_optin)
         return TMC_E_INVALID;
     std::lock_guard<std::mutex> lk(api_mutex());
-    const bool replan = block != b->cfg.block || (cfg->items_per_block ? cfg->items_per_block : 8) !=
+    bool replan = block != b->cfg.block || (cfg->items_per_block ? cfg->items_per_block : 8) !=
                                                     b->cfg.items_per_block;
     b->cfg.block = block;
     b->cfg.items_per_block = cfg->items_per_block ? cfg->items_per_block : 8;
@@ -472,6 +484,14 @@ int tmc_batch_set_config(tmc_batch *b, const tmc_batch_config *cfg)
         b->graph = nullptr;
     }
     b->cfg.use_graph = cfg->use_graph ? 1 : 0;
+    if (b->cfg.stream != (cfg->stream ? 1 : 0)) {
+        b->cfg.stream = cfg->stream ? 1 : 0;
+        replan = true;
+        if (b->graph) {
+            cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+        }
+    }
     if (replan)
         b->planned = false;
     return TMC_OK;
@@ -503,6 +523,13 @@ int tmc_batch_read(tmc_batch *b, tmc_tally *tallies, uint64_t *steps_per_problem
         return st;
     cudaError_t e = cudaStreamSynchronize(b->last_stream);
     const size_t n = b->problems.size();
+    unsigned long long err = 0;
+    if (e == cudaSuccess)
+        e = cudaMemcpy(&err, b->d_counter + 1, sizeof err, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && err) {
+        set_error_text("tmc_batch_read: a bounded device wait ran out");
+        return TMC_E_TIMEOUT;
+    }
     if (e == cudaSuccess && tallies)
         e = cudaMemcpy(tallies, b->d_tally, sizeof(tmc_tally) * b->offsets[n], cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && steps_per_problem && n)
@@ -575,15 +602,17 @@ int tmc_batch_autotune(tmc_batch *b, double scale, double max_steps_per_photon, 
         return st;
     static const int blocks[3] = {128, 256, 512};
     static const int ipb[3] = {4, 8, 16};
+    static const int streams[2] = {0, 1};
     double best = 1e300;
     tmc_batch_config best_cfg = b->cfg;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaError_t e = cudaEventCreate(&e0);
     if (e == cudaSuccess)
         e = cudaEventCreate(&e1);
-    for (int bi = 0; bi < 3 && e == cudaSuccess && st == TMC_OK; ++bi) {
-        for (int ii = 0; ii < 3 && e == cudaSuccess && st == TMC_OK; ++ii) {
-            tmc_batch_config c{blocks[bi], ipb[ii], 0};
+    for (int k = 0; k < 18 && e == cudaSuccess && st == TMC_OK; ++k) {
+        {
+            const int bi = k % 3, ii = (k / 3) % 3, si = k / 9;
+            tmc_batch_config c{blocks[bi], ipb[ii], 0, streams[si]};
             if (tmc_batch_set_config(t, &c) != TMC_OK)
                 continue;
             st = tmc_batch_run(t, nullptr);          // warm-up and planning
@@ -599,6 +628,8 @@ int tmc_batch_autotune(tmc_batch *b, double scale, double max_steps_per_photon, 
             float ms = 0.f;
             if (e == cudaSuccess)
                 e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e == cudaSuccess && st == TMC_OK)
+                st = tmc_batch_read(t, nullptr, nullptr);   // error flag of the run
             if (e == cudaSuccess && st == TMC_OK && ms < best) {
                 best = ms;
                 best_cfg = c;

@@ -34,6 +34,7 @@ struct BatchArgs {
     unsigned long long *steps;         // [problems]
     unsigned long long *item_counter;  // zero at launch
     unsigned long long *item_probe;    // [n_items][2] (128-bit, lo then hi) or null
+    unsigned *error;                   // walk_stream: set to 1 when a bounded wait ran out
 };
 
 size_t walk_batch_smem(uint32_t max_shells, int block);
@@ -41,5 +42,10 @@ size_t walk_batch_smem(uint32_t max_shells, int block);
 cudaError_t walk_batch_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid);
 // Launch only (capturable); walk_batch_prepare must have run for this shape.
 cudaError_t walk_batch_launch(const BatchArgs &a, int block, uint32_t math, int grid, cudaStream_t s);
+
+// The barrier-free variant (tmc_stream.cu): two open items per block.
+size_t walk_stream_smem(uint32_t max_shells, int block);
+cudaError_t walk_stream_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid);
+cudaError_t walk_stream_launch(const BatchArgs &a, int block, uint32_t math, int grid, cudaStream_t s);
 
 }  // namespace tmc

@@ -77,6 +77,7 @@ struct Wave {
     unsigned long long *d_counter = nullptr;
     BatchItemDev *h_items = nullptr;        // pinned
     unsigned long long *h_probe = nullptr;  // pinned
+    unsigned long long *h_err = nullptr;    // pinned: the wave's error flag
     uint32_t n_items = 0;
     bool busy = false;
 };
@@ -127,6 +128,7 @@ void destroy_server(tmc_server *s)
         cudaFree(w.d_counter);
         cudaFreeHost(w.h_items);
         cudaFreeHost(w.h_probe);
+        cudaFreeHost(w.h_err);
     }
     if (s->admin)
         cudaStreamDestroy(s->admin);
@@ -238,6 +240,10 @@ int decide(tmc_server *s, uint64_t id)
 // Harvest a completed wave: store per-item values, decide where possible.
 int harvest(tmc_server *s, Wave &w)
 {
+    if (*w.h_err) {
+        set_error_text("server wave: a bounded device wait ran out");
+        return TMC_E_TIMEOUT;
+    }
     std::vector<uint64_t> touched;
     for (uint32_t i = 0; i < w.n_items; ++i) {
         const BatchItemDev &it = w.h_items[i];
@@ -300,8 +306,8 @@ int launch_wave(tmc_server *s, Wave &w)
     w.n_items = n;
     cudaError_t e = cudaMemcpyAsync(w.d_items, w.h_items, sizeof(BatchItemDev) * n,
                                     cudaMemcpyHostToDevice, w.stream);
-    if (e == cudaSuccess)
-        e = cudaMemsetAsync(w.d_counter, 0, sizeof(unsigned long long), w.stream);
+    if (e == cudaSuccess)   // item counter and error flag
+        e = cudaMemsetAsync(w.d_counter, 0, 2 * sizeof(unsigned long long), w.stream);
     if (e == cudaSuccess) {
         BatchArgs a;
         a.keys = s->keys;
@@ -314,9 +320,17 @@ int launch_wave(tmc_server *s, Wave &w)
         a.steps = s->d_steps;
         a.item_counter = w.d_counter;
         a.item_probe = w.d_probe;
-        e = walk_batch_launch(a, (int)s->cfg.block, s->cfg.math, std::max(1, std::min<int>(s->grid, (int)n)),
-                              w.stream);
+        a.error = reinterpret_cast<unsigned *>(w.d_counter + 1);
+        if (s->cfg.stream)
+            e = walk_stream_launch(a, (int)s->cfg.block, s->cfg.math,
+                                   std::max(1, std::min<int>(s->grid, (int)((n + 1) / 2))), w.stream);
+        else
+            e = walk_batch_launch(a, (int)s->cfg.block, s->cfg.math,
+                                  std::max(1, std::min<int>(s->grid, (int)n)), w.stream);
     }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(w.h_err, w.d_counter + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                            w.stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(w.h_probe, w.d_probe, 2 * sizeof(unsigned long long) * n,
                             cudaMemcpyDeviceToHost, w.stream);
@@ -393,11 +407,14 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
     s->device = c->device;
     s->sms = c->sms;
     s->keys = make_philox_keys(cfg->seed);
-    if (walk_batch_smem(cfg->max_shells, (int)cfg->block) > c->smem_optin) {
-        set_error_text("tmc_server_create: max_shells too large for the shared-memory histogram");
+    const size_t smem = cfg->stream ? walk_stream_smem(cfg->max_shells, (int)cfg->block)
+                                    : walk_batch_smem(cfg->max_shells, (int)cfg->block);
+    if (smem > c->smem_optin) {
+        set_error_text("tmc_server_create: max_shells too large for the shared-memory histograms");
         return TMC_E_INVALID;
     }
-    cudaError_t e = walk_batch_prepare((int)cfg->block, cfg->math, cfg->max_shells, c->sms, &s->grid);
+    cudaError_t e = cfg->stream ? walk_stream_prepare((int)cfg->block, cfg->math, cfg->max_shells, c->sms, &s->grid)
+                                : walk_batch_prepare((int)cfg->block, cfg->math, cfg->max_shells, c->sms, &s->grid);
     if (e != cudaSuccess)
         return set_cuda_error(e, "server kernel config");
     const size_t slots = cfg->slots;
@@ -421,7 +438,9 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
         if (e == cudaSuccess)
             e = cudaMalloc(&w.d_probe, 2 * sizeof(unsigned long long) * s->items_cap);
         if (e == cudaSuccess)
-            e = cudaMalloc(&w.d_counter, sizeof(unsigned long long));
+            e = cudaMalloc(&w.d_counter, 2 * sizeof(unsigned long long));
+        if (e == cudaSuccess)
+            e = cudaMallocHost(&w.h_err, sizeof(unsigned long long));
         if (e == cudaSuccess)
             e = cudaMallocHost(&w.h_items, sizeof(BatchItemDev) * s->items_cap);
         if (e == cudaSuccess)

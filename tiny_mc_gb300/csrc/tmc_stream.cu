@@ -1,0 +1,407 @@
+// tmc_stream.cu — the batched walk without per-item barriers.
+//
+// walk_batch (tmc_batch.cu) walks one work item per block at a time: every
+// warp of the block waits at a barrier for the slowest lane of the item before
+// the block takes the next one.  With heavy-tailed walk lengths those waits
+// idle a large part of the block.  walk_stream keeps TWO items open per block,
+// each with its own shared-memory histogram:
+//
+//  * a warp claims photons from its current item j; when j has no photons
+//    left, lanes that need a photon take it from item j+1 as soon as the
+//    block has opened it, while the other lanes finish their photons of j.
+//    Each lane deposits into the histogram of its own photon's item, so a
+//    warp spans at most two items;
+//  * a warp reports an item done when the item has no photons left and none
+//    of its lanes still walks one; the last warp of the block to report item
+//    j flushes j's histogram into the problem's 128-bit tally, writes the
+//    item's probe value, zeroes the histogram, claims the next global item
+//    for it (j+2) and publishes it;
+//  * waits (a warp with nothing to walk until the block opens the next item)
+//    are bounded by wall time through %globaltimer: past the limit the warp
+//    sets the error flag and leaves; the host reports TMC_E_TIMEOUT.
+// Results are bit-identical to walk_batch and the plain kernel: the same
+// photons, integer sums.
+#include <algorithm>
+
+#include "tmc_batch.cuh"
+#include "tmc_internal.h"
+#include "tmc_walk.cuh"
+
+namespace tmc {
+
+namespace {
+
+constexpr uint32_t END_ITEM = 0xffffffffu;
+constexpr unsigned long long WAIT_LIMIT_NS = 120ull * 1000000000ull;
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+struct OpenItem {           // per buffer, in shared memory
+    uint32_t item;          // global item index, or END_ITEM
+    uint32_t next;          // photon counter within the item
+    uint32_t done;          // warps that reported the item
+    uint32_t wraps;         // 2^64 wraps of the probe shell's sum
+    uint32_t gen;           // item sequence number this buffer holds
+};
+
+__device__ __forceinline__ uint32_t claim_global_item(const BatchArgs &a)
+{
+    const unsigned long long it = atomicAdd(a.item_counter, 1ull);
+    return it < a.n_items ? (uint32_t)it : END_ITEM;
+}
+
+}  // namespace
+
+template <int BLOCK, class M>
+__global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
+{
+    constexpr unsigned NWARPS = BLOCK / 32;
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ OpenItem open[2];
+    const uint32_t HS = 4 * a.max_shells;          // words per histogram
+    uint32_t *my = smem + 2 * HS + threadIdx.x;    // ring slot k: my[k * BLOCK]
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt_mask = (1u << lane) - 1u;
+
+    for (uint32_t s = threadIdx.x; s < 2 * HS; s += BLOCK)
+        smem[s] = 0;
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < 2; ++b) {
+            open[b].item = claim_global_item(a);
+            open[b].next = 0;
+            open[b].done = 0;
+            open[b].wraps = 0;
+            open[b].gen = (uint32_t)b;
+        }
+    }
+    __syncthreads();
+    volatile OpenItem *vopen = open;
+
+    // ---- warp-uniform state
+    uint32_t jc = 0;          // item sequence the warp claims photons from
+    uint32_t rep = 0;         // lowest item sequence this warp has not reported
+    bool exh = false;         // item jc has no photons left
+    uint32_t cn = 0, ce = 0;  // current chunk of photon indices within item jc
+    // item jc's description (warp-uniform copies)
+    uint32_t it_c = open[0].item;
+    BatchItemDev item_c{};
+    BatchProblemDev pr_c{};
+    if (it_c != END_ITEM) {
+        item_c = a.items[it_c];
+        pr_c = a.problems[item_c.problem];
+    }
+
+    // ---- lane state
+    bool alive = false, want = true, pending = false;
+    uint32_t pid_lo = 0, pid_hi = 0, blk = 0, prod = 0, cur = 0;
+    float x = 0.f, y = 0.f, z = 0.f, u = 0.f, v = 0.f, w = 1.f, weight = 1.f;
+    uint32_t lb = 0;                          // buffer of this lane's photon
+    WalkConsts c{};                           // optics of this lane's photon
+    unsigned long long *g = nullptr;          // its problem's global tally
+    uint32_t ps = 0;                          // its probe shell
+    uint32_t steps0 = 0, steps1 = 0;          // steps walked per buffer
+    unsigned long long wait_start = 0;
+
+    for (;;) {
+        // -------- report items this warp is finished with (oldest first)
+        for (;;) {
+            if (rep > jc || (rep == jc && !exh))
+                break;
+            const uint32_t rb = rep & 1u;
+            if (vopen[rb].item == END_ITEM)
+                break;
+            if (__any_sync(FULL_MASK, alive && lb == rb))
+                break;
+            // this warp's steps on that item, then the done count (after its
+            // lanes' deposits into the item's histogram are ordered before it)
+            const unsigned long long st = warp_sum_u64(rb ? steps1 : steps0);
+            if (rb)
+                steps1 = 0;
+            else
+                steps0 = 0;
+            const uint32_t it = vopen[rb].item;
+            const BatchItemDev itm = a.items[it];
+            unsigned last = 0;
+            __syncwarp();
+            __threadfence_block();
+            if (lane == 0) {
+                if (st)
+                    atomicAdd(&a.steps[itm.problem], st);
+                last = (atomicAdd((unsigned *)&open[rb].done, 1u) == NWARPS - 1) ? 1u : 0u;
+            }
+            last = __shfl_sync(FULL_MASK, last, 0);
+            if (last) {
+                // every warp is done with item `rep`: flush, probe, reset, reopen
+                __threadfence_block();
+                const BatchProblemDev pr = a.problems[itm.problem];
+                const uint32_t S = pr.c.shells;
+                uint32_t *hist = smem + rb * HS;
+                unsigned long long *gg = a.tally + 4 * pr.tally_offset;
+                for (uint32_t s = lane; s < S; s += 32) {
+                    flush128(&gg[4 * s + 0], &gg[4 * s + 1],
+                             ((unsigned long long)hist[S + s] << 32) | hist[s]);
+                    flush128(&gg[4 * s + 2], &gg[4 * s + 3],
+                             ((unsigned long long)hist[3 * S + s] << 32) | hist[2 * S + s]);
+                }
+                if (a.item_probe && lane == 0) {
+                    const uint32_t p = min(a.probe_shell, S - 1);
+                    a.item_probe[2 * (size_t)it] = ((unsigned long long)hist[S + p] << 32) | hist[p];
+                    a.item_probe[2 * (size_t)it + 1] = vopen[rb].wraps;
+                }
+                __syncwarp();
+                for (uint32_t s = lane; s < 4 * S; s += 32)
+                    hist[s] = 0;
+                uint32_t nxt = 0;
+                if (lane == 0)
+                    nxt = claim_global_item(a);
+                nxt = __shfl_sync(FULL_MASK, nxt, 0);
+                if (lane == 0) {
+                    vopen[rb].item = nxt;
+                    vopen[rb].next = 0;
+                    vopen[rb].done = 0;
+                    vopen[rb].wraps = 0;
+                    __threadfence_block();
+                    vopen[rb].gen = rep + 2;
+                }
+                __syncwarp();
+            }
+            ++rep;
+        }
+
+        // -------- hand photons to lanes that want one
+        unsigned need = __ballot_sync(FULL_MASK, want);
+        bool waiting = false;
+        while (need) {
+            if (it_c == END_ITEM)
+                break;
+            if (!exh) {
+                const unsigned n_need = __popc(need);
+                const unsigned rank = __popc(need & lt_mask);
+                uint32_t k = min((uint32_t)n_need, ce - cn);
+                if (k == 0) {
+                    uint32_t base = 0;
+                    if (lane == 0)
+                        base = atomicAdd((unsigned *)&open[jc & 1u].next, (uint32_t)BATCH_CHUNK);
+                    base = __shfl_sync(FULL_MASK, base, 0);
+                    if (base >= item_c.count) {
+                        exh = true;
+                        continue;
+                    }
+                    cn = base;
+                    ce = min(base + (uint32_t)BATCH_CHUNK, item_c.count);
+                    k = min((uint32_t)n_need, ce - cn);
+                }
+                const bool mine = ((need >> lane) & 1u) && rank < k;
+                if (mine) {
+                    // launch, photon.c:12-18
+                    const unsigned long long pid = pr_c.id_base + item_c.first + (cn + rank);
+                    pid_lo = (uint32_t)pid;
+                    pid_hi = (uint32_t)(pid >> 32);
+                    want = false;
+                    alive = true;
+                    blk = 0;
+                    cur = prod;
+                    pending = false;
+                    x = y = z = 0.f;
+                    u = v = 0.f;
+                    w = 1.f;
+                    weight = 1.f;
+                    lb = jc & 1u;
+                    c = pr_c.c;
+                    g = a.tally + 4 * pr_c.tally_offset;
+                    ps = min(a.probe_shell, pr_c.c.shells - 1);
+                }
+                cn += k;
+                need = __ballot_sync(FULL_MASK, want);
+                continue;
+            }
+            // item jc is used up: move on once the block has opened jc+1
+            const uint32_t nb = (jc + 1) & 1u;
+            if (vopen[nb].gen != jc + 1) {
+                waiting = true;
+                break;
+            }
+            __threadfence_block();
+            ++jc;
+            exh = false;
+            cn = ce = 0;
+            it_c = vopen[nb].item;
+            if (it_c != END_ITEM) {
+                item_c = a.items[it_c];
+                pr_c = a.problems[item_c.problem];
+            }
+        }
+        if (it_c == END_ITEM && need) {
+            // no more work for lanes that want a photon
+            want = false;
+        }
+
+        const bool any_alive = __any_sync(FULL_MASK, alive);
+        if (!any_alive) {
+            if (it_c == END_ITEM && rep >= jc)
+                break;   // all photons walked, all items reported
+            // nothing to walk until the block opens the next item
+            if (wait_start == 0)
+                wait_start = global_ns();
+            else if (global_ns() - wait_start > WAIT_LIMIT_NS) {
+                if (lane == 0)
+                    atomicExch(a.error, 1u);
+                break;
+            }
+            __nanosleep(waiting ? 200 : 50);
+            continue;
+        }
+        wait_start = 0;
+
+        // -------- keep >= 6 random words buffered (one iteration uses <= 6)
+        while (__any_sync(FULL_MASK, alive && (prod - cur) < 6u)) {
+            if (alive && (prod - cur) <= (uint32_t)(RING - 4)) {
+                const uint4 r = philox4x32_10(blk, 0u, pid_lo, pid_hi, a.keys);
+                ++blk;
+                const uint32_t p = prod & (RING - 1);
+                uint32_t *dst = my + p * BLOCK;
+                dst[0 * BLOCK] = r.x;
+                dst[1 * BLOCK] = r.y;
+                dst[2 * BLOCK] = r.z;
+                dst[3 * BLOCK] = r.w;
+                uint32_t *mir = dst + RING * BLOCK;
+                if (p <= 4u) {
+                    mir[0 * BLOCK] = r.x;
+                    mir[1 * BLOCK] = r.y;
+                }
+                if (p == 0u) {
+                    mir[2 * BLOCK] = r.z;
+                    mir[3 * BLOCK] = r.w;
+                }
+                prod += 4;
+            }
+        }
+
+        if (alive) {
+            const uint32_t *rd = my + (cur & (RING - 1)) * BLOCK;
+            if (!pending) {
+                // move, photon.c:21-24
+                const float U = uniform01(rd[0]);
+                rd += BLOCK;
+                ++cur;
+                const float t = M::step_length(U);
+                x = M::move(x, t, u);
+                y = M::move(y, t, v);
+                z = M::move(z, t, w);
+                // absorb, photon.c:26-32
+                const float rr = M::radius_shells(x, y, z, c.spm);
+                const uint32_t shell = __float2uint_rz(fminf(rr, c.last));
+                const uint32_t S = c.shells;
+                uint32_t *t0 = smem + lb * HS + shell;
+                uint32_t lo, hi;
+                fx40_split(weight, lo, hi);
+                tally_add(t0, t0 + S, &g[4 * shell + 1], lo, hi,
+                          shell == ps ? (uint32_t *)&open[lb].wraps : nullptr);
+                fx40_split(__fmul_rn(weight, weight), lo, hi);
+                tally_add(t0 + 2 * S, t0 + 3 * S, &g[4 * shell + 3], lo, hi);
+                weight = M::mul(weight, c.albedo);
+                steps1 += lb;
+                steps0 += 1u - lb;
+            }
+            // the next two tries of the rejection method, photon.c:36-40
+            const float xa1 = uniform_pm1(rd[0 * BLOCK]);
+            const float xa2 = uniform_pm1(rd[1 * BLOCK]);
+            const float xb1 = uniform_pm1(rd[2 * BLOCK]);
+            const float xb2 = uniform_pm1(rd[3 * BLOCK]);
+            const float ta = M::norm2(xa1, xa2);
+            const float tb = M::norm2(xb1, xb2);
+            const bool first = !(1.0f < ta);
+            const float xi1 = first ? xa1 : xb1;
+            const float xi2 = first ? xa2 : xb2;
+            const float tt = first ? ta : tb;
+            rd += first ? 2 * BLOCK : 4 * BLOCK;
+            cur += first ? 2u : 4u;
+            pending = (1.0f < tt);
+            if (!pending) {
+                // new direction, photon.c:41-43
+                u = fmaf(2.0f, tt, -1.0f);
+                const float sc = M::dir_scale(tt, u);
+                v = M::mul(xi1, sc);
+                w = M::mul(xi2, sc);
+                // roulette, photon.c:45-49
+                if (weight < 0.001f) {
+                    const float U = uniform01(rd[0]);
+                    ++cur;
+                    if (U > 0.1f) {
+                        alive = false;
+                        want = true;
+                    } else {
+                        weight = __fdiv_rn(weight, 0.1f);
+                    }
+                }
+            }
+        }
+    }
+}
+
+size_t walk_stream_smem(uint32_t max_shells, int block)
+{
+    return (size_t)32 * max_shells + (size_t)4 * SLOTS * block;
+}
+
+template <int BLOCK, class M>
+static cudaError_t stream_config(int sms, size_t smem, int *grid)
+{
+    auto kern = walk_stream<BLOCK, M>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, smem);
+    if (e != cudaSuccess)
+        return e;
+    if (per_sm < 1)
+        return cudaErrorInvalidConfiguration;
+    *grid = sms * per_sm;
+    return cudaSuccess;
+}
+
+cudaError_t walk_stream_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid)
+{
+    const size_t smem = walk_stream_smem(max_shells, block);
+    const bool fast = math == TMC_MATH_FAST;
+    switch (block) {
+    case 128: return fast ? stream_config<128, FastMath>(sms, smem, grid)
+                          : stream_config<128, ExactMath>(sms, smem, grid);
+    case 256: return fast ? stream_config<256, FastMath>(sms, smem, grid)
+                          : stream_config<256, ExactMath>(sms, smem, grid);
+    case 512: return fast ? stream_config<512, FastMath>(sms, smem, grid)
+                          : stream_config<512, ExactMath>(sms, smem, grid);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t walk_stream_launch(const BatchArgs &a, int block, uint32_t math, int grid, cudaStream_t s)
+{
+    const size_t smem = walk_stream_smem(a.max_shells, block);
+    const bool fast = math == TMC_MATH_FAST;
+    switch (block) {
+    case 128:
+        if (fast) walk_stream<128, FastMath><<<grid, 128, smem, s>>>(a);
+        else walk_stream<128, ExactMath><<<grid, 128, smem, s>>>(a);
+        break;
+    case 256:
+        if (fast) walk_stream<256, FastMath><<<grid, 256, smem, s>>>(a);
+        else walk_stream<256, ExactMath><<<grid, 256, smem, s>>>(a);
+        break;
+    case 512:
+        if (fast) walk_stream<512, FastMath><<<grid, 512, smem, s>>>(a);
+        else walk_stream<512, ExactMath><<<grid, 512, smem, s>>>(a);
+        break;
+    default:
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace tmc

@@ -27,7 +27,7 @@ class ServerConfig(ctypes.Structure):
     _fields_ = [("slots", ctypes.c_uint32), ("max_shells", ctypes.c_uint32),
                 ("probe_shell", ctypes.c_uint32), ("min_batches", ctypes.c_uint32),
                 ("seed", ctypes.c_uint64), ("math", ctypes.c_uint32), ("block", ctypes.c_uint32),
-                ("max_items_per_request", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("max_items_per_request", ctypes.c_uint32), ("stream", ctypes.c_uint32),
                 ("steps_per_batch", ctypes.c_double)]
 
 
