@@ -65,6 +65,8 @@ def parse():
                     help="plain: config 1 (default); sweep: the 4096-problem batched sweep; "
                          "serve: the request stream")
     ap.add_argument("--serve-slots", type=int, default=1024)
+    ap.add_argument("--serve-stream", type=int, choices=[-1, 0, 1], default=-1,
+                    help="server kernel: 0 per-item barriers, 1 barrier-free, -1 library default")
     ap.add_argument("--serve-calib", type=int, default=256)
     ap.add_argument("--serve-window", type=float, default=10.0)
     ap.add_argument("--serve-duration", type=float, default=60.0)
@@ -497,7 +499,8 @@ def run_serve(args):
     torch.cuda.set_device(0)
     n_total = 100000
     req, arr = make_trace(n_total, rate=2000.0, seed=0)
-    s = Server(slots=args.serve_slots, math=1 if args.math == "fast" else 0)
+    kw = {} if args.serve_stream < 0 else {"stream": args.serve_stream}
+    s = Server(slots=args.serve_slots, math=1 if args.math == "fast" else 0, **kw)
     # 1. calibration
     C = args.serve_calib
     t0 = time.perf_counter()
@@ -523,7 +526,8 @@ def run_serve(args):
     lat_o = res_o["latency_s"][got]
     s.close()
     # 3. slowed to 70 % of capacity
-    s = Server(slots=args.serve_slots, math=1 if args.math == "fast" else 0)
+    s = Server(slots=args.serve_slots, math=1 if args.math == "fast" else 0, **kw)
+    kernel = "barrier-free" if s.cfg.stream else "per-item barriers"
     rate = 0.7 * saturated / mean_steps
     n3 = max(50, min(int(rate * args.serve_duration), n_total - C))
     sel3 = slice(C, C + n3)
@@ -544,7 +548,8 @@ def run_serve(args):
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": "served stream (config 4): Poisson arrivals, target RSE at shell 10 "
                                "in [0.5%, 5%], cap 2^24 photons, sweep parameter distribution",
-                   "trace_seed": 0, "math": args.math, "slots": args.serve_slots},
+                   "trace_seed": 0, "math": args.math, "slots": args.serve_slots,
+                   "kernel": kernel},
         "latency_p50_s": pct(lat, 50), "latency_p99_s": pct(lat, 99),
         "photon_steps_per_s": steps3 / t_s,
         "requests": n3, "completed": int(done_s), "arrival_rate_per_s": rate,

@@ -298,7 +298,7 @@ cudaError_t enqueue(const tmc_batch *b, cudaStream_t s)
     a.error = reinterpret_cast<unsigned *>(b->d_counter + 1);
     if (b->cfg.stream) {
         // two items open per block: no more blocks than half the items
-        const int grid = std::max(1, std::min<int>(b->grid, (int)((b->n_items + 1) / 2)));
+        const int grid = std::max(1, std::min<int>(b->grid, (int)b->n_items));
         return walk_stream_launch(a, b->cfg.block, b->math, grid, s);
     }
     const int grid = std::max(1, std::min<int>(b->grid, (int)b->n_items));

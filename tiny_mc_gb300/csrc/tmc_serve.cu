@@ -323,7 +323,7 @@ int launch_wave(tmc_server *s, Wave &w)
         a.error = reinterpret_cast<unsigned *>(w.d_counter + 1);
         if (s->cfg.stream)
             e = walk_stream_launch(a, (int)s->cfg.block, s->cfg.math,
-                                   std::max(1, std::min<int>(s->grid, (int)((n + 1) / 2))), w.stream);
+                                   std::max(1, std::min<int>(s->grid, (int)n)), w.stream);
         else
             e = walk_batch_launch(a, (int)s->cfg.block, s->cfg.math,
                                   std::max(1, std::min<int>(s->grid, (int)n)), w.stream);

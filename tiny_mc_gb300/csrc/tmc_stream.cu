@@ -3,22 +3,26 @@
 // walk_batch (tmc_batch.cu) walks one work item per block at a time: every
 // warp of the block waits at a barrier for the slowest lane of the item before
 // the block takes the next one.  With heavy-tailed walk lengths those waits
-// idle a large part of the block.  walk_stream keeps TWO items open per block,
-// each with its own shared-memory histogram:
+// idle a large part of the block.  walk_stream keeps up to TWO items open per
+// block, each in a buffer with its own shared-memory histogram:
 //
 //  * a warp claims photons from its current item j; when j has no photons
-//    left, lanes that need a photon take it from item j+1 as soon as the
-//    block has opened it, while the other lanes finish their photons of j.
-//    Each lane deposits into the histogram of its own photon's item, so a
-//    warp spans at most two items;
+//    left, lanes that need a photon take them from item j+1, which the first
+//    warp to get there claims from the global queue (so a block never holds
+//    an item it has not started), while the other lanes finish their photons
+//    of j.  Each lane deposits into the histogram of its own photon's item,
+//    so a warp spans at most two items;
 //  * a warp reports an item done when the item has no photons left and none
 //    of its lanes still walks one; the last warp of the block to report item
 //    j flushes j's histogram into the problem's 128-bit tally, writes the
-//    item's probe value, zeroes the histogram, claims the next global item
-//    for it (j+2) and publishes it;
-//  * waits (a warp with nothing to walk until the block opens the next item)
-//    are bounded by wall time through %globaltimer: past the limit the warp
-//    sets the error flag and leaves; the host reports TMC_E_TIMEOUT.
+//    item's probe value and step count, zeroes the histogram and frees the
+//    buffer for item j+2;
+//  * the item's optics, tally pointer and photon ids live in the buffer's
+//    shared record, not in registers, so the kernel keeps the plain walk's
+//    occupancy; photon steps are added to the record when a photon dies;
+//  * waits (a warp with nothing to walk until the block frees a buffer) are
+//    bounded by wall time through %globaltimer: past the limit the warp sets
+//    the error flag and leaves; the host reports TMC_E_TIMEOUT.
 // Results are bit-identical to walk_batch and the plain kernel: the same
 // photons, integer sums.
 #include <algorithm>
@@ -33,6 +37,7 @@ namespace {
 
 constexpr uint32_t END_ITEM = 0xffffffffu;
 constexpr unsigned long long WAIT_LIMIT_NS = 120ull * 1000000000ull;
+constexpr uint32_t BUF_FREE = 0, BUF_CLAIMING = 1, BUF_OPEN = 2;
 
 __device__ __forceinline__ unsigned long long global_ns()
 {
@@ -41,18 +46,40 @@ __device__ __forceinline__ unsigned long long global_ns()
     return t;
 }
 
-struct OpenItem {           // per buffer, in shared memory
-    uint32_t item;          // global item index, or END_ITEM
-    uint32_t next;          // photon counter within the item
-    uint32_t done;          // warps that reported the item
-    uint32_t wraps;         // 2^64 wraps of the probe shell's sum
-    uint32_t gen;           // item sequence number this buffer holds
+struct __align__(16) OpenItem {    // per buffer, in shared memory
+    WalkConsts c;                  // optics of the item's problem
+    unsigned long long *g;         // the problem's 128-bit global tally
+    unsigned long long id_first;   // photon id of the item's first photon
+    uint32_t item;                 // global item index, or END_ITEM
+    uint32_t count;                // photons in the item
+    uint32_t ps;                   // probe shell, clamped to the problem
+    uint32_t next;                 // photon counter within the item
+    uint32_t done;                 // warps that reported the item
+    uint32_t wraps;                // 2^64 wraps of the probe shell's sum
+    uint32_t steps_lo, steps_hi;   // photon steps walked on the item
+    uint32_t gen;                  // item sequence number the buffer is for
+    uint32_t state;                // BUF_FREE / BUF_CLAIMING / BUF_OPEN
 };
 
-__device__ __forceinline__ uint32_t claim_global_item(const BatchArgs &a)
+// Claim the next global item into buffer o (one thread).
+__device__ __forceinline__ void open_item(const BatchArgs &a, OpenItem *o)
 {
     const unsigned long long it = atomicAdd(a.item_counter, 1ull);
-    return it < a.n_items ? (uint32_t)it : END_ITEM;
+    o->item = it < a.n_items ? (uint32_t)it : END_ITEM;
+    if (it < a.n_items) {
+        const BatchItemDev itm = a.items[it];
+        const BatchProblemDev pr = a.problems[itm.problem];
+        o->c = pr.c;
+        o->g = a.tally + 4 * pr.tally_offset;
+        o->id_first = pr.id_base + itm.first;
+        o->count = itm.count;
+        o->ps = min(a.probe_shell, pr.c.shells - 1);
+    }
+    o->next = 0;
+    o->done = 0;
+    o->wraps = 0;
+    o->steps_lo = 0;
+    o->steps_hi = 0;
 }
 
 }  // namespace
@@ -71,13 +98,11 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
     for (uint32_t s = threadIdx.x; s < 2 * HS; s += BLOCK)
         smem[s] = 0;
     if (threadIdx.x == 0) {
-        for (int b = 0; b < 2; ++b) {
-            open[b].item = claim_global_item(a);
-            open[b].next = 0;
-            open[b].done = 0;
-            open[b].wraps = 0;
-            open[b].gen = (uint32_t)b;
-        }
+        open_item(a, &open[0]);
+        open[0].gen = 0;
+        open[0].state = BUF_OPEN;
+        open[1].gen = 1;
+        open[1].state = BUF_FREE;
     }
     __syncthreads();
     volatile OpenItem *vopen = open;
@@ -87,24 +112,14 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
     uint32_t rep = 0;         // lowest item sequence this warp has not reported
     bool exh = false;         // item jc has no photons left
     uint32_t cn = 0, ce = 0;  // current chunk of photon indices within item jc
-    // item jc's description (warp-uniform copies)
     uint32_t it_c = open[0].item;
-    BatchItemDev item_c{};
-    BatchProblemDev pr_c{};
-    if (it_c != END_ITEM) {
-        item_c = a.items[it_c];
-        pr_c = a.problems[item_c.problem];
-    }
 
     // ---- lane state
     bool alive = false, want = true, pending = false;
     uint32_t pid_lo = 0, pid_hi = 0, blk = 0, prod = 0, cur = 0;
     float x = 0.f, y = 0.f, z = 0.f, u = 0.f, v = 0.f, w = 1.f, weight = 1.f;
     uint32_t lb = 0;                          // buffer of this lane's photon
-    WalkConsts c{};                           // optics of this lane's photon
-    unsigned long long *g = nullptr;          // its problem's global tally
-    uint32_t ps = 0;                          // its probe shell
-    uint32_t steps0 = 0, steps1 = 0;          // steps walked per buffer
+    uint32_t steps = 0;                       // steps of this lane's photon
     unsigned long long wait_start = 0;
 
     for (;;) {
@@ -117,54 +132,45 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
                 break;
             if (__any_sync(FULL_MASK, alive && lb == rb))
                 break;
-            // this warp's steps on that item, then the done count (after its
-            // lanes' deposits into the item's histogram are ordered before it)
-            const unsigned long long st = warp_sum_u64(rb ? steps1 : steps0);
-            if (rb)
-                steps1 = 0;
-            else
-                steps0 = 0;
-            const uint32_t it = vopen[rb].item;
-            const BatchItemDev itm = a.items[it];
+            // the done count, after this warp's deposits into the item
             unsigned last = 0;
             __syncwarp();
             __threadfence_block();
-            if (lane == 0) {
-                if (st)
-                    atomicAdd(&a.steps[itm.problem], st);
+            if (lane == 0)
                 last = (atomicAdd((unsigned *)&open[rb].done, 1u) == NWARPS - 1) ? 1u : 0u;
-            }
             last = __shfl_sync(FULL_MASK, last, 0);
             if (last) {
-                // every warp is done with item `rep`: flush, probe, reset, reopen
+                // every warp is done with item `rep`: flush, probe, reset, free
                 __threadfence_block();
-                const BatchProblemDev pr = a.problems[itm.problem];
-                const uint32_t S = pr.c.shells;
+                const uint32_t it = vopen[rb].item;
+                const uint32_t S = vopen[rb].c.shells;
                 uint32_t *hist = smem + rb * HS;
-                unsigned long long *gg = a.tally + 4 * pr.tally_offset;
+                unsigned long long *gg = open[rb].g;
                 for (uint32_t s = lane; s < S; s += 32) {
                     flush128(&gg[4 * s + 0], &gg[4 * s + 1],
                              ((unsigned long long)hist[S + s] << 32) | hist[s]);
                     flush128(&gg[4 * s + 2], &gg[4 * s + 3],
                              ((unsigned long long)hist[3 * S + s] << 32) | hist[2 * S + s]);
                 }
-                if (a.item_probe && lane == 0) {
-                    const uint32_t p = min(a.probe_shell, S - 1);
-                    a.item_probe[2 * (size_t)it] = ((unsigned long long)hist[S + p] << 32) | hist[p];
-                    a.item_probe[2 * (size_t)it + 1] = vopen[rb].wraps;
+                if (lane == 0) {
+                    const unsigned long long st =
+                        ((unsigned long long)vopen[rb].steps_hi << 32) | vopen[rb].steps_lo;
+                    if (st)
+                        atomicAdd(&a.steps[a.items[it].problem], st);
+                    if (a.item_probe) {
+                        const uint32_t p = vopen[rb].ps;
+                        a.item_probe[2 * (size_t)it] =
+                            ((unsigned long long)hist[S + p] << 32) | hist[p];
+                        a.item_probe[2 * (size_t)it + 1] = vopen[rb].wraps;
+                    }
                 }
                 __syncwarp();
                 for (uint32_t s = lane; s < 4 * S; s += 32)
                     hist[s] = 0;
-                uint32_t nxt = 0;
-                if (lane == 0)
-                    nxt = claim_global_item(a);
-                nxt = __shfl_sync(FULL_MASK, nxt, 0);
+                __threadfence_block();
+                __syncwarp();
                 if (lane == 0) {
-                    vopen[rb].item = nxt;
-                    vopen[rb].next = 0;
-                    vopen[rb].done = 0;
-                    vopen[rb].wraps = 0;
+                    vopen[rb].state = BUF_FREE;
                     __threadfence_block();
                     vopen[rb].gen = rep + 2;
                 }
@@ -179,6 +185,7 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
         while (need) {
             if (it_c == END_ITEM)
                 break;
+            const uint32_t cb = jc & 1u;
             if (!exh) {
                 const unsigned n_need = __popc(need);
                 const unsigned rank = __popc(need & lt_mask);
@@ -186,20 +193,21 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
                 if (k == 0) {
                     uint32_t base = 0;
                     if (lane == 0)
-                        base = atomicAdd((unsigned *)&open[jc & 1u].next, (uint32_t)BATCH_CHUNK);
+                        base = atomicAdd((unsigned *)&open[cb].next, (uint32_t)BATCH_CHUNK);
                     base = __shfl_sync(FULL_MASK, base, 0);
-                    if (base >= item_c.count) {
+                    const uint32_t count = open[cb].count;
+                    if (base >= count) {
                         exh = true;
                         continue;
                     }
                     cn = base;
-                    ce = min(base + (uint32_t)BATCH_CHUNK, item_c.count);
+                    ce = min(base + (uint32_t)BATCH_CHUNK, count);
                     k = min((uint32_t)n_need, ce - cn);
                 }
                 const bool mine = ((need >> lane) & 1u) && rank < k;
                 if (mine) {
                     // launch, photon.c:12-18
-                    const unsigned long long pid = pr_c.id_base + item_c.first + (cn + rank);
+                    const unsigned long long pid = open[cb].id_first + (cn + rank);
                     pid_lo = (uint32_t)pid;
                     pid_hi = (uint32_t)(pid >> 32);
                     want = false;
@@ -211,18 +219,30 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
                     u = v = 0.f;
                     w = 1.f;
                     weight = 1.f;
-                    lb = jc & 1u;
-                    c = pr_c.c;
-                    g = a.tally + 4 * pr_c.tally_offset;
-                    ps = min(a.probe_shell, pr_c.c.shells - 1);
+                    lb = cb;
+                    steps = 0;
                 }
                 cn += k;
                 need = __ballot_sync(FULL_MASK, want);
                 continue;
             }
-            // item jc is used up: move on once the block has opened jc+1
-            const uint32_t nb = (jc + 1) & 1u;
-            if (vopen[nb].gen != jc + 1) {
+            // item jc is used up: move on to sequence jc+1 once its buffer is
+            // free, claiming its item if no warp of the block has yet
+            const uint32_t nb = cb ^ 1u;
+            uint32_t st = BUF_FREE;
+            if (lane == 0 && vopen[nb].gen == jc + 1) {
+                __threadfence_block();
+                st = vopen[nb].state;
+                if (st == BUF_FREE &&
+                    atomicCAS((unsigned *)&open[nb].state, BUF_FREE, BUF_CLAIMING) == BUF_FREE) {
+                    open_item(a, &open[nb]);
+                    __threadfence_block();
+                    vopen[nb].state = BUF_OPEN;
+                    st = BUF_OPEN;
+                }
+            }
+            st = __shfl_sync(FULL_MASK, st, 0);
+            if (st != BUF_OPEN) {
                 waiting = true;
                 break;
             }
@@ -231,10 +251,6 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
             exh = false;
             cn = ce = 0;
             it_c = vopen[nb].item;
-            if (it_c != END_ITEM) {
-                item_c = a.items[it_c];
-                pr_c = a.problems[item_c.problem];
-            }
         }
         if (it_c == END_ITEM && need) {
             // no more work for lanes that want a photon
@@ -245,7 +261,7 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
         if (!any_alive) {
             if (it_c == END_ITEM && rep >= jc)
                 break;   // all photons walked, all items reported
-            // nothing to walk until the block opens the next item
+            // nothing to walk until the block frees a buffer
             if (wait_start == 0)
                 wait_start = global_ns();
             else if (global_ns() - wait_start > WAIT_LIMIT_NS) {
@@ -283,6 +299,7 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
         }
 
         if (alive) {
+            const OpenItem &o = open[lb];
             const uint32_t *rd = my + (cur & (RING - 1)) * BLOCK;
             if (!pending) {
                 // move, photon.c:21-24
@@ -294,19 +311,20 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
                 y = M::move(y, t, v);
                 z = M::move(z, t, w);
                 // absorb, photon.c:26-32
+                const WalkConsts c = o.c;
                 const float rr = M::radius_shells(x, y, z, c.spm);
                 const uint32_t shell = __float2uint_rz(fminf(rr, c.last));
                 const uint32_t S = c.shells;
                 uint32_t *t0 = smem + lb * HS + shell;
+                unsigned long long *g = o.g;
                 uint32_t lo, hi;
                 fx40_split(weight, lo, hi);
                 tally_add(t0, t0 + S, &g[4 * shell + 1], lo, hi,
-                          shell == ps ? (uint32_t *)&open[lb].wraps : nullptr);
+                          shell == o.ps ? (uint32_t *)&open[lb].wraps : nullptr);
                 fx40_split(__fmul_rn(weight, weight), lo, hi);
                 tally_add(t0 + 2 * S, t0 + 3 * S, &g[4 * shell + 3], lo, hi);
                 weight = M::mul(weight, c.albedo);
-                steps1 += lb;
-                steps0 += 1u - lb;
+                ++steps;
             }
             // the next two tries of the rejection method, photon.c:36-40
             const float xa1 = uniform_pm1(rd[0 * BLOCK]);
@@ -335,6 +353,11 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
                     if (U > 0.1f) {
                         alive = false;
                         want = true;
+                        // the photon's steps into its item's 64-bit count
+                        uint32_t *sl = (uint32_t *)&open[lb].steps_lo;
+                        const uint32_t old = atomicAdd(sl, steps);
+                        if (old + steps < old)
+                            atomicAdd((uint32_t *)&open[lb].steps_hi, 1u);
                     } else {
                         weight = __fdiv_rn(weight, 0.1f);
                     }
