@@ -65,6 +65,8 @@ def parse():
                     help="plain: config 1 (default); sweep: the 4096-problem batched sweep; "
                          "serve: the request stream")
     ap.add_argument("--serve-slots", type=int, default=1024)
+    ap.add_argument("--serve-steps-per-batch", type=float, default=0.0,
+                    help="server RSE batch size in photon steps (0: library default)")
     ap.add_argument("--serve-stream", type=int, choices=[-1, 0, 1], default=-1,
                     help="server kernel: 0 per-item barriers, 1 barrier-free, -1 library default")
     ap.add_argument("--serve-calib", type=int, default=256)
@@ -500,6 +502,8 @@ def run_serve(args):
     n_total = 100000
     req, arr = make_trace(n_total, rate=2000.0, seed=0)
     kw = {} if args.serve_stream < 0 else {"stream": args.serve_stream}
+    if args.serve_steps_per_batch > 0:
+        kw["steps_per_batch"] = args.serve_steps_per_batch
     s = Server(slots=args.serve_slots, math=1 if args.math == "fast" else 0, **kw)
     # 1. calibration
     C = args.serve_calib
@@ -549,7 +553,7 @@ def run_serve(args):
         "config": {"workload": "served stream (config 4): Poisson arrivals, target RSE at shell 10 "
                                "in [0.5%, 5%], cap 2^24 photons, sweep parameter distribution",
                    "trace_seed": 0, "math": args.math, "slots": args.serve_slots,
-                   "kernel": kernel},
+                   "kernel": kernel, "steps_per_batch": s.cfg.steps_per_batch},
         "latency_p50_s": pct(lat, 50), "latency_p99_s": pct(lat, 99),
         "photon_steps_per_s": steps3 / t_s,
         "requests": n3, "completed": int(done_s), "arrival_rate_per_s": rate,

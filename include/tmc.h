@@ -220,7 +220,7 @@ typedef struct tmc_batch_config {
     int block;            /* threads per block: 128, 256 or 512 (0 = 256) */
     int items_per_block;  /* work items per resident block: load-balance granularity (0 = 8) */
     int use_graph;        /* 1: run through a captured CUDA graph, replayed on later runs */
-    int stream;           /* 1: two items open per block, lanes flow into the next item
+    int stream;           /* 1: up to two items open per block, lanes flow into the next item
                              instead of waiting at a barrier for the slowest lane */
 } tmc_batch_config;
 
@@ -228,7 +228,8 @@ int tmc_batch_create(tmc_batch **out, const tmc_problem *problems, uint32_t n_pr
                      uint64_t seed, uint32_t math);
 int tmc_batch_set_config(tmc_batch *b, const tmc_batch_config *cfg);
 int tmc_batch_get_config(const tmc_batch *b, tmc_batch_config *cfg);
-/* Times block size x items-per-block candidates on a reduced copy of the batch
+/* Times block size x items-per-block x kernel (stream 0/1) candidates on a
+ * reduced copy of the batch
  * (photon counts x scale, problems above max_steps_per_photon expected steps
  * left out; 0 = keep all) and keeps the fastest.  best_ms may be NULL. */
 int tmc_batch_autotune(tmc_batch *b, double scale, double max_steps_per_photon, double *best_ms);
@@ -288,7 +289,7 @@ typedef struct tmc_server_config {
     uint32_t math;
     uint32_t block;                 /* 128, 256 or 512 */
     uint32_t max_items_per_request; /* RSE batches of one request in one wave */
-    uint32_t stream;                /* 1: barrier-free kernel (two items open per block) */
+    uint32_t stream;                /* 1: barrier-free kernel (up to two items open per block) */
     double steps_per_batch;         /* target photon steps per RSE batch */
 } tmc_server_config;
 

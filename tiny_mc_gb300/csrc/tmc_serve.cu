@@ -139,11 +139,14 @@ void destroy_server(tmc_server *s)
 }
 
 // Photons per RSE batch: a power of two near steps_per_batch / E[steps], in
-// [2 x block, 65536]: at least two photons per thread of the block walking it.
+// [lo, 65536].  lo is two photons per thread of the block for the kernel with
+// per-item barriers (fewer would idle the block at the barrier), and one
+// warp's claim (BATCH_CHUNK) for the barrier-free kernel, whose lanes move on
+// to the next item.
 uint32_t batch_photons(const tmc_server_config &cfg, double est_steps)
 {
     const double want = cfg.steps_per_batch / std::max(1.0, est_steps);
-    uint32_t b = 2 * cfg.block;
+    uint32_t b = cfg.stream ? (uint32_t)BATCH_CHUNK : 2 * cfg.block;
     while (b < 65536 && 2.0 * b <= want)
         b *= 2;
     return b;
