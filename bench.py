@@ -38,6 +38,13 @@ METRIC = "photons/s on 1 GB300 (plain vs batched/served) at stated error; p50/p9
 UNIT = "photons/s"
 SFU_OPS_PER_STEP = 4          # log, sqrt (radius), divide + sqrt (direction)
 CPU_PHOTONS_PER_PROC = 1 << 16
+# Issue-slot accounting of walk_plain<256, FastMath> at config-1 optics, from
+# ncu --set full of one 2^25-photon launch (profiles/walk_plain_fast_
+# 2p25photons_ncu_full.txt): thread-instructions per photon step and the busy
+# fraction of each pipe.  An SM issues at most 4 warp-instructions per clock.
+WALK_THREAD_INSTR_PER_STEP = 229.6
+WALK_PIPES_NCU = {"issue_slots": 0.796, "alu": 0.543, "fma_heavy": 0.522, "xu_sfu": 0.199,
+                  "shared_wavefronts": 0.504, "dram": 0.0}
 # DRAM bytes (read + write) of one walk launch, from an ncu capture of the walk
 # at config-1 optics (2^25 photons): only the 101-shell tally flush touches
 # DRAM, so the figure does not grow with the photon count.
@@ -75,6 +82,8 @@ def parse():
     ap.add_argument("--serve-drain", type=float, default=120.0)
     ap.add_argument("--sweep-scale", type=float, default=1.0 / 64,
                     help="photon-count multiplier of the sweep (1 = full size, ~3.3e13 steps)")
+    ap.add_argument("--batch-config", default="",
+                    help="sweep: fixed 'block,items_per_block,stream' instead of the autotuner")
     ap.add_argument("--plain-steps", type=int, default=1,
                     help="sweep workload: timed passes of the one-launch-per-problem form")
     return ap.parse_args()
@@ -349,6 +358,18 @@ def run_ours(args):
         "photon_steps_per_launch": photon_steps / args.steps,
         "peak_source": "measured live: MUFU lg2/sqrt/rcp probe (tmc_probe_sfu_rate)",
     }
+    # the pipe that binds: instruction issue (4 warp-instructions per clock per
+    # SM); its ceiling at the sampled clock, and the ncu pipe utilisations
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
+    if mhz and args.optics == "cfg1" and args.math == "fast":
+        issue_steps = props.multi_processor_count * mhz * 1e6 * 4 * 32 / WALK_THREAD_INSTR_PER_STEP
+        roofline["binding_pipe"] = {
+            "pipe": "instruction issue", "thread_instr_per_step": WALK_THREAD_INSTR_PER_STEP,
+            "ceiling_photon_steps_per_s": issue_steps,
+            "frac": (photon_steps / args.steps / per_launch_s) / issue_steps,
+            "sm_mhz": mhz, "pipes_busy_ncu": WALK_PIPES_NCU,
+            "source": "ncu --set full, profiles/walk_plain_fast_2p25photons_ncu_full.txt",
+        }
 
     # the exact (bit-reproducible) arithmetic on the same workload, for reference
     value_exact = None
@@ -419,8 +440,20 @@ def run_sweep(args):
     photons = int(sw["n_photons"].sum())
     b = tmc.Batch(sw, seed=1, math=args.math)
     t0 = time.perf_counter()
-    tune_ms = b.autotune(scale=min(1.0, 1.0 / 16), max_steps_per_photon=2e4)
+    if args.batch_config:
+        blk, ipb, strm = (int(v) for v in args.batch_config.split(","))
+        b.set_config(blk, ipb, False, bool(strm))
+        tune_ms = None
+    else:
+        tune_ms = b.autotune(scale=min(1.0, 1.0 / 16), max_steps_per_photon=2e4)
     tune_s = time.perf_counter() - t0
+    refine_ms, refine_s = None, None
+    if not args.batch_config and args.sweep_scale <= 1.0 / 16:
+        # second stage on the batch itself (4 full runs; skipped at large
+        # scales, where each run takes minutes)
+        t0 = time.perf_counter()
+        refine_ms = b.refine(4)
+        refine_s = time.perf_counter() - t0
     b.set_config(**{**b.config(), "use_graph": True})
     _, est_steps = b.info()
     stream = torch.cuda.current_stream()
@@ -469,7 +502,8 @@ def run_sweep(args):
                    "photon_steps_per_step": photon_steps,
                    "est_photon_steps_per_step": est_steps, "math": args.math,
                    "sweep_seed": 0, "rng_seed": 1, "batch_config": b.config(), "work_items": n_items,
-                   "autotune_s": tune_s, "autotune_best_ms": tune_ms},
+                   "autotune_s": tune_s, "autotune_best_ms": tune_ms,
+                   "refine_s": refine_s, "refine_best_ms": refine_ms},
         "photon_steps_per_s": photon_steps * args.steps / (sum(ms) * 1e-3),
         "plain_form": ({"value": plain, "unit": UNIT, "ms_per_pass": sum(plain_ms) / len(plain_ms),
                         "launches_per_pass": len(sw)} if plain_ms else None),

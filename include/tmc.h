@@ -233,6 +233,14 @@ int tmc_batch_get_config(const tmc_batch *b, tmc_batch_config *cfg);
  * (photon counts x scale, problems above max_steps_per_photon expected steps
  * left out; 0 = keep all) and keeps the fastest.  best_ms may be NULL. */
 int tmc_batch_autotune(tmc_batch *b, double scale, double max_steps_per_photon, double *best_ms);
+/* Second tuning stage, on the batch itself: takes the fastest configuration
+ * of each (kernel, block size) from the last tmc_batch_autotune, at most
+ * max_candidates of them in order, times one full run of each and keeps the
+ * fastest (a reduced copy cannot rank them: how much the longest single
+ * photons weigh depends on the batch's size).  Costs max_candidates runs;
+ * results do not depend on the configuration.  TMC_E_STATE if autotune has
+ * not run.  Not in the reference (it has no batched form). */
+int tmc_batch_refine(tmc_batch *b, uint32_t max_candidates, double *best_ms);
 /* Zeroes the batch's device tallies and walks every problem (asynchronous on
  * stream, a cudaStream_t or NULL). */
 int tmc_batch_run(tmc_batch *b, void *stream);

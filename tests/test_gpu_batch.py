@@ -101,10 +101,19 @@ def test_batch_autotune_keeps_results(tmc_mod):
     b = tmc_mod.Batch(sw, seed=4, math="fast")
     b.run()
     ref, _ = b.read()
+    with pytest.raises(tmc_mod.TmcError):
+        b.refine(4)                    # TMC_E_STATE: no autotune yet
     ms = b.autotune(scale=0.25, max_steps_per_photon=2e4)
     assert ms > 0
     cfg = b.config()
-    assert cfg["block"] in (128, 256, 512) and cfg["items_per_block"] in (4, 8, 16)
+    assert cfg["block"] in (128, 256, 512) and cfg["items_per_block"] in (4, 8, 16, 64)
+    b.run()
+    t, _ = b.read()
+    assert np.array_equal(t, ref)
+    b.set_config(**{**b.config(), "use_graph": True})
+    assert b.refine(4) > 0
+    cfg = b.config()
+    assert cfg["use_graph"] is True and cfg["block"] in (128, 256, 512)
     b.run()
     t, _ = b.read()
     assert np.array_equal(t, ref)

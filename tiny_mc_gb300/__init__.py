@@ -103,6 +103,8 @@ def lib() -> ctypes.CDLL:
         L.tmc_batch_get_config.restype = i32
         L.tmc_batch_autotune.argtypes = [vp, ctypes.c_double, ctypes.c_double, vp]
         L.tmc_batch_autotune.restype = i32
+        L.tmc_batch_refine.argtypes = [vp, ctypes.c_uint32, vp]
+        L.tmc_batch_refine.restype = i32
         L.tmc_batch_run.argtypes = [vp, vp]
         L.tmc_batch_run.restype = i32
         L.tmc_batch_read.argtypes = [vp, vp, vp]
@@ -251,6 +253,13 @@ class Batch:
         ms = ctypes.c_double(0.0)
         _check(lib().tmc_batch_autotune(self.handle, scale, max_steps_per_photon, ctypes.byref(ms)),
                "tmc_batch_autotune")
+        return ms.value
+
+    def refine(self, max_candidates: int = 4) -> float:
+        """Second tuning stage: the best autotuned configuration of each
+        (kernel, block size), one full run each; keeps the fastest."""
+        ms = ctypes.c_double(0.0)
+        _check(lib().tmc_batch_refine(self.handle, max_candidates, ctypes.byref(ms)), "tmc_batch_refine")
         return ms.value
 
     def run(self, stream: int = 0) -> None:

@@ -194,6 +194,8 @@ struct tmc_batch {
     cudaStream_t capture_stream = nullptr;
     cudaStream_t last_stream = nullptr;
     bool planned = false;
+    // configurations timed by the last autotune on the reduced copy (ms, config)
+    std::vector<std::pair<double, tmc_batch_config>> tuned;
 };
 
 namespace {
@@ -221,12 +223,20 @@ int plan(tmc_batch *b)
     for (size_t i = 0; i < b->problems.size(); ++i)
         total += b->est_steps[i] * (double)b->problems[i].n_photons;
     const double target = std::max(1.0, total / ((double)grid * std::max(1, b->cfg.items_per_block)));
-    const unsigned long long min_item = (unsigned long long)b->cfg.block * 2;
+    // Smallest item: two photons per thread of the block (a lane whose first
+    // photon dies early takes a second one), or one photon per thread for a
+    // problem whose photons are so long (high albedo: up to ~1e6 steps, each
+    // walked serially by one lane) that two of them in a row would reach the
+    // launch's expected steps per lane: spread one per lane, such photons
+    // start in the first items and do not set the end of the launch.
+    const double lane_steps = total / ((double)grid * b->cfg.block);
     std::vector<std::pair<double, BatchItemDev>> items;
     for (size_t i = 0; i < b->problems.size(); ++i) {
         const unsigned long long n = b->problems[i].n_photons;
         if (n == 0)
             continue;
+        const unsigned long long min_item =
+            (unsigned long long)b->cfg.block * (2.0 * b->est_steps[i] <= lane_steps ? 2 : 1);
         const double work = b->est_steps[i] * (double)n;
         unsigned long long k = (unsigned long long)std::ceil(work / target);
         k = std::max(1ull, std::min(k, (n + min_item - 1) / min_item));
@@ -601,17 +611,18 @@ int tmc_batch_autotune(tmc_batch *b, double scale, double max_steps_per_photon, 
     if (st)
         return st;
     static const int blocks[3] = {128, 256, 512};
-    static const int ipb[3] = {4, 8, 16};
+    static const int ipb[4] = {4, 8, 16, 64};
     static const int streams[2] = {0, 1};
     double best = 1e300;
     tmc_batch_config best_cfg = b->cfg;
+    b->tuned.clear();
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaError_t e = cudaEventCreate(&e0);
     if (e == cudaSuccess)
         e = cudaEventCreate(&e1);
-    for (int k = 0; k < 18 && e == cudaSuccess && st == TMC_OK; ++k) {
+    for (int k = 0; k < 24 && e == cudaSuccess && st == TMC_OK; ++k) {
         {
-            const int bi = k % 3, ii = (k / 3) % 3, si = k / 9;
+            const int bi = k % 3, ii = (k / 3) % 4, si = k / 12;
             tmc_batch_config c{blocks[bi], ipb[ii], 0, streams[si]};
             if (tmc_batch_set_config(t, &c) != TMC_OK)
                 continue;
@@ -630,6 +641,8 @@ int tmc_batch_autotune(tmc_batch *b, double scale, double max_steps_per_photon, 
                 e = cudaEventElapsedTime(&ms, e0, e1);
             if (e == cudaSuccess && st == TMC_OK)
                 st = tmc_batch_read(t, nullptr, nullptr);   // error flag of the run
+            if (e == cudaSuccess && st == TMC_OK)
+                b->tuned.push_back({(double)ms, c});
             if (e == cudaSuccess && st == TMC_OK && ms < best) {
                 best = ms;
                 best_cfg = c;
@@ -646,6 +659,70 @@ int tmc_batch_autotune(tmc_batch *b, double scale, double max_steps_per_photon, 
     if (e != cudaSuccess)
         return set_cuda_error(e, "tmc_batch_autotune");
     best_cfg.use_graph = b->cfg.use_graph;
+    st = tmc_batch_set_config(b, &best_cfg);
+    if (best_ms)
+        *best_ms = best;
+    return st;
+}
+
+int tmc_batch_refine(tmc_batch *b, uint32_t max_candidates, double *best_ms)
+{
+    if (!b || max_candidates == 0)
+        return TMC_E_INVALID;
+    if (b->tuned.empty())
+        return TMC_E_STATE;
+    // the fastest reduced-copy configuration of each (kernel, block size)
+    std::vector<std::pair<double, tmc_batch_config>> cand(b->tuned);
+    std::stable_sort(cand.begin(), cand.end(),
+                     [](const auto &x, const auto &y) { return x.first < y.first; });
+    std::vector<tmc_batch_config> pick;
+    for (const auto &c : cand) {
+        bool seen = false;
+        for (const auto &q : pick)
+            seen = seen || (q.block == c.second.block && q.stream == c.second.stream);
+        if (!seen && pick.size() < max_candidates)
+            pick.push_back(c.second);
+    }
+    const int use_graph = b->cfg.use_graph;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e1);
+    int st = TMC_OK;
+    double best = 1e300;
+    tmc_batch_config best_cfg = b->cfg;
+    for (size_t k = 0; k < pick.size() && e == cudaSuccess && st == TMC_OK; ++k) {
+        tmc_batch_config c = pick[k];
+        c.use_graph = 0;
+        st = tmc_batch_set_config(b, &c);
+        if (st)
+            break;
+        e = cudaEventRecord(e0, nullptr);
+        if (e == cudaSuccess)
+            st = tmc_batch_run(b, nullptr);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(e1, nullptr);
+        if (e == cudaSuccess)
+            e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess)
+            e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess && st == TMC_OK)
+            st = tmc_batch_read(b, nullptr, nullptr);
+        if (e == cudaSuccess && st == TMC_OK && ms < best) {
+            best = ms;
+            best_cfg = c;
+        }
+    }
+    if (e0)
+        cudaEventDestroy(e0);
+    if (e1)
+        cudaEventDestroy(e1);
+    if (st)
+        return st;
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "tmc_batch_refine");
+    best_cfg.use_graph = use_graph;
     st = tmc_batch_set_config(b, &best_cfg);
     if (best_ms)
         *best_ms = best;

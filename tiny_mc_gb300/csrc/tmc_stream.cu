@@ -181,7 +181,6 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
 
         // -------- hand photons to lanes that want one
         unsigned need = __ballot_sync(FULL_MASK, want);
-        bool waiting = false;
         while (need) {
             if (it_c == END_ITEM)
                 break;
@@ -242,10 +241,8 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
                 }
             }
             st = __shfl_sync(FULL_MASK, st, 0);
-            if (st != BUF_OPEN) {
-                waiting = true;
+            if (st != BUF_OPEN)
                 break;
-            }
             __threadfence_block();
             ++jc;
             exh = false;
@@ -261,15 +258,18 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
         if (!any_alive) {
             if (it_c == END_ITEM && rep >= jc)
                 break;   // all photons walked, all items reported
-            // nothing to walk until the block frees a buffer
+            // nothing to walk until the block frees a buffer: sleep about an
+            // eighth of the time waited so far (64 ns .. 16 us), so waiting
+            // warps leave the issue slots to the block's walking warps
+            const unsigned long long now = global_ns();
             if (wait_start == 0)
-                wait_start = global_ns();
-            else if (global_ns() - wait_start > WAIT_LIMIT_NS) {
+                wait_start = now;
+            else if (now - wait_start > WAIT_LIMIT_NS) {
                 if (lane == 0)
                     atomicExch(a.error, 1u);
                 break;
             }
-            __nanosleep(waiting ? 200 : 50);
+            __nanosleep(64u + (unsigned)min((now - wait_start) >> 3, 16384ull));
             continue;
         }
         wait_start = 0;
