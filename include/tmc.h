@@ -59,7 +59,7 @@ typedef enum tmc_math {
 
 /* Runtime form of params.h's knobs. */
 typedef struct tmc_params {
-    uint32_t shells;            /* SHELLS            (params.h:5-7),   >= 1      */
+    uint32_t shells;            /* SHELLS            (params.h:5-7),   1 .. 2^24 */
     float microns_per_shell;    /* MICRONS_PER_SHELL (params.h:21-23), > 0       */
     float mu_a;                 /* MU_A, 1/cm        (params.h:13-15), > 0       */
     float mu_s;                 /* MU_S, 1/cm        (params.h:17-19), >= 0      */

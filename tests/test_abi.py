@@ -56,6 +56,16 @@ def test_invalid_params_rejected_before_any_launch(tmc_mod, field, value):
     assert not heat.any()
 
 
+def test_shell_count_limit(tmc_mod):
+    """1 .. 2^24 shells: above that (float)(shells - 1), the clamp bound of
+    photon.c:27-29 done in float, would no longer be exact."""
+    import ctypes
+    p = tmc_mod.params(shells=(1 << 24) + 1)
+    heat = np.zeros(101, np.float32)
+    st = tmc_mod.lib().tmc_photon_batch(heat.ctypes.data, heat.ctypes.data, 10, ctypes.byref(p))
+    assert st == -1 and not heat.any()
+
+
 def test_null_arrays_rejected(tmc_mod):
     p = tmc_mod.params()
     assert tmc_mod.lib().tmc_photon_batch(None, None, 1, ctypes.byref(p)) == -1

@@ -80,6 +80,20 @@ def test_exact_bit_identical_random_optics(tmc_mod, oracle_mod):
         assert np.array_equal(got, ref), optics
 
 
+@pytest.mark.parametrize("shells,mps,n,nt", [(20000, 0.5, 4096, 0), (1 << 24, 0.001, 64, 1)])
+def test_exact_bit_identical_wide_tallies(tmc_mod, oracle_mod, shells, mps, n, nt):
+    """Shell counts whose histogram does not fit in shared memory: deposits go
+    straight to the 128-bit global tally; up to the 2^24-shell maximum, where
+    (float)(shells - 1) is still exact for the clamp of photon.c:27-29."""
+    optics = dict(shells=shells, microns_per_shell=mps, mu_a=2.0, mu_s=20.0)
+    got, steps = gpu_fx(tmc_mod, n, seed=5, **optics)
+    p = oracle_mod.oparams(shells, mps, 2.0, 20.0, 5)
+    ref, dep, ref_steps = oracle_mod.walk_fx(p, n, nthreads=nt)
+    assert steps == ref_steps
+    assert np.array_equal(got, ref)
+    assert int((dep > 0).sum()) > 1000          # deposits spread over many shells
+
+
 @pytest.mark.parametrize("n", [0, 1, 31, 32, 33, 255, 257, 4097])
 def test_edge_photon_counts(tmc_mod, oracle_mod, n):
     got, steps = gpu_fx(tmc_mod, n, seed=3, **CFG0)

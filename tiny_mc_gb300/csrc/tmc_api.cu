@@ -222,10 +222,9 @@ static int run_into_ctx_tally(DeviceCtx &c, uint64_t n, const tmc_params *p, con
 
 static int check_sizes(uint64_t n, const tmc_params *p, const DeviceCtx &c)
 {
+    (void)c;
     if (n > (1ull << 62) || p->photon_id_base > ~0ull - n)
         return TMC_E_OVERFLOW;
-    if ((int64_t)p->shells > plain_max_shells(c))
-        return TMC_E_INVALID;
     return TMC_OK;
 }
 

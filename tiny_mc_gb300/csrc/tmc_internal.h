@@ -60,6 +60,8 @@ struct PlainLaunch {
 };
 cudaError_t launch_plain(const PlainLaunch &L, const DeviceCtx &ctx, cudaStream_t stream);
 size_t plain_smem_bytes(uint32_t shells, int block);
+// Largest shell count whose shared-memory histogram fits at the default
+// block; launch_plain walks larger counts with global-memory deposits.
 int plain_max_shells(const DeviceCtx &ctx);
 
 // FP64 finalisation on the device (tmc_api.cu).

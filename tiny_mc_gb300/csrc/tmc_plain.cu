@@ -3,7 +3,10 @@
 // Reference path: tiny_mc.c:47-49 calls photon() (photon.c:6-51) once per
 // photon.  Here a persistent grid walks all n photons with the loop in
 // tmc_walk.cuh; each block owns a shared-memory histogram of the problem's
-// shells and adds it to the 128-bit global tally once at the end.
+// shells and adds it to the 128-bit global tally once at the end.  Shell
+// counts whose histogram does not fit in shared memory (params.h's SHELLS is
+// any size in the reference) take the WIDE form: deposits go straight into the
+// 128-bit global tally with 64-bit atomics; the sums are the same integers.
 #include <algorithm>
 
 #include "tmc_internal.h"
@@ -23,11 +26,11 @@ struct PlainArgs {
     unsigned long long *steps;   // += photon steps, may be null
 };
 
-template <int BLOCK, class M>
+template <int BLOCK, class M, bool WIDE>
 __global__ void __launch_bounds__(BLOCK) walk_plain(const PlainArgs a)
 {
     extern __shared__ __align__(16) uint32_t smem[];
-    const uint32_t S = a.c.shells;
+    const uint32_t S = WIDE ? 0u : a.c.shells;   // histogram words / 4
     for (uint32_t s = threadIdx.x; s < 4 * S; s += BLOCK)
         smem[s] = 0;
     __syncthreads();
@@ -37,10 +40,13 @@ __global__ void __launch_bounds__(BLOCK) walk_plain(const PlainArgs a)
     src.n = a.n_photons;
     src.id_base = a.id_base;
     uint32_t *my = smem + 4 * S + threadIdx.x;   // ring slot k: my[k * BLOCK]
-    const uint32_t steps = walk_loop<BLOCK, M>(a.c, src, a.keys, smem, a.tally, my);
+    const uint32_t steps =
+        walk_loop<BLOCK, M, GlobalSource<CHUNK>, WIDE>(a.c, src, a.keys, smem, a.tally, my);
 
-    __syncthreads();
-    flush_tally<BLOCK>(smem, S, a.tally);
+    if constexpr (!WIDE) {
+        __syncthreads();
+        flush_tally<BLOCK>(smem, S, a.tally);
+    }
     if (a.steps) {
         const unsigned long long tot = warp_sum_u64(steps);
         if ((threadIdx.x & 31u) == 0 && tot)
@@ -53,18 +59,24 @@ size_t plain_smem_bytes(uint32_t shells, int block)
     return (size_t)16 * shells + (size_t)4 * SLOTS * block;
 }
 
-int plain_max_shells(const DeviceCtx &ctx)
+// Largest shell count whose histogram fits beside a block's ring buffers.
+static uint32_t histogram_max_shells(const DeviceCtx &ctx, int block)
 {
     const size_t cap = ctx.smem_optin ? ctx.smem_optin : 48 * 1024;
-    const size_t ring = (size_t)4 * SLOTS * 256;
-    return cap > ring ? (int)((cap - ring) / 16) : 0;
+    const size_t ring = (size_t)4 * SLOTS * block;
+    return cap > ring ? (uint32_t)((cap - ring) / 16) : 0u;
 }
 
-template <int BLOCK, class M>
+int plain_max_shells(const DeviceCtx &ctx)
+{
+    return (int)histogram_max_shells(ctx, 256);
+}
+
+template <int BLOCK, class M, bool WIDE>
 static cudaError_t launch_t(const PlainLaunch &L, const DeviceCtx &ctx, cudaStream_t stream)
 {
-    const size_t smem = plain_smem_bytes(L.d.shells, BLOCK);
-    auto kern = walk_plain<BLOCK, M>;
+    const size_t smem = plain_smem_bytes(WIDE ? 0u : L.d.shells, BLOCK);
+    auto kern = walk_plain<BLOCK, M, WIDE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess)
@@ -100,19 +112,24 @@ static cudaError_t launch_t(const PlainLaunch &L, const DeviceCtx &ctx, cudaStre
     return cudaGetLastError();
 }
 
+template <int BLOCK>
+static cudaError_t launch_b(const PlainLaunch &L, const DeviceCtx &ctx, cudaStream_t stream)
+{
+    const bool fast = L.p->math == TMC_MATH_FAST;
+    if (L.d.shells <= histogram_max_shells(ctx, BLOCK))
+        return fast ? launch_t<BLOCK, FastMath, false>(L, ctx, stream)
+                    : launch_t<BLOCK, ExactMath, false>(L, ctx, stream);
+    return fast ? launch_t<BLOCK, FastMath, true>(L, ctx, stream)
+                : launch_t<BLOCK, ExactMath, true>(L, ctx, stream);
+}
+
 cudaError_t launch_plain(const PlainLaunch &L, const DeviceCtx &ctx, cudaStream_t stream)
 {
-    const int block = L.block ? L.block : 256;
-    const bool fast = L.p->math == TMC_MATH_FAST;
-    switch (block) {
-    case 128:
-        return fast ? launch_t<128, FastMath>(L, ctx, stream) : launch_t<128, ExactMath>(L, ctx, stream);
-    case 256:
-        return fast ? launch_t<256, FastMath>(L, ctx, stream) : launch_t<256, ExactMath>(L, ctx, stream);
-    case 512:
-        return fast ? launch_t<512, FastMath>(L, ctx, stream) : launch_t<512, ExactMath>(L, ctx, stream);
-    default:
-        return cudaErrorInvalidValue;
+    switch (L.block ? L.block : 256) {
+    case 128: return launch_b<128>(L, ctx, stream);
+    case 256: return launch_b<256>(L, ctx, stream);
+    case 512: return launch_b<512>(L, ctx, stream);
+    default: return cudaErrorInvalidValue;
     }
 }
 

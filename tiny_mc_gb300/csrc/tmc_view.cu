@@ -182,8 +182,6 @@ int tmc_progressive_create(tmc_progressive **out, const tmc_params *p)
     DeviceCtx *c = current_ctx(&st);
     if (!c)
         return st;
-    if ((int64_t)p->shells > plain_max_shells(*c))
-        return TMC_E_INVALID;
     std::unique_ptr<tmc_progressive, void (*)(tmc_progressive *)> g(new tmc_progressive,
                                                                     destroy_progressive);
     g->p = *p;

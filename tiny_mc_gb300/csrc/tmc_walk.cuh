@@ -142,7 +142,10 @@ struct SharedSource {
 // sum w^2); g: the problem's global 128-bit tally [shells][4] (receives only
 // carries here).  probe_wraps (may be null): counts the 2^64 wraps of the
 // block's sum of w in shell probe_shell.  Returns this thread's photon steps.
-template <int BLOCK, class M, class Source>
+// WIDE: no shared histogram (tally unused); every deposit is a 64-bit atomic
+// add into g with the carry into the high word, for shell counts whose
+// histogram does not fit in shared memory.
+template <int BLOCK, class M, class Source, bool WIDE = false>
 __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
                                               const PhiloxKeys &keys, uint32_t *tally,
                                               unsigned long long *g, uint32_t *my,
@@ -225,13 +228,20 @@ __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
                 // radius below 2^32 shells, and a NaN radius lands last)
                 const float rr = M::radius_shells(x, y, z, c.spm);
                 const uint32_t shell = __float2uint_rz(fminf(rr, c.last));
-                uint32_t *t0 = tally + shell;
                 uint32_t lo, hi;
-                fx40_split(weight, lo, hi);
-                tally_add(t0, t0 + S, &g[4 * shell + 1], lo, hi,
-                          shell == probe_shell ? probe_wraps : nullptr);
-                fx40_split(__fmul_rn(weight, weight), lo, hi);
-                tally_add(t0 + 2 * S, t0 + 3 * S, &g[4 * shell + 3], lo, hi);
+                if constexpr (WIDE) {
+                    fx40_split(weight, lo, hi);
+                    flush128(&g[4 * shell + 0], &g[4 * shell + 1], ((unsigned long long)hi << 32) | lo);
+                    fx40_split(__fmul_rn(weight, weight), lo, hi);
+                    flush128(&g[4 * shell + 2], &g[4 * shell + 3], ((unsigned long long)hi << 32) | lo);
+                } else {
+                    uint32_t *t0 = tally + shell;
+                    fx40_split(weight, lo, hi);
+                    tally_add(t0, t0 + S, &g[4 * shell + 1], lo, hi,
+                              shell == probe_shell ? probe_wraps : nullptr);
+                    fx40_split(__fmul_rn(weight, weight), lo, hi);
+                    tally_add(t0 + 2 * S, t0 + 3 * S, &g[4 * shell + 3], lo, hi);
+                }
                 weight = M::mul(weight, c.albedo);
                 ++steps;
             }
