@@ -74,6 +74,12 @@ def parse():
     ap.add_argument("--serve-slots", type=int, default=1024)
     ap.add_argument("--serve-steps-per-batch", type=float, default=0.0,
                     help="server RSE batch size in photon steps (0: library default)")
+    ap.add_argument("--serve-steps-per-item", type=float, default=-1.0,
+                    help="server work item size in photon steps (0: one item per batch; -1: library default)")
+    ap.add_argument("--serve-inflight-items", type=int, default=-1,
+                    help="server cap on launched, unfinished work items (0: none; -1: library default)")
+    ap.add_argument("--serve-waves", type=int, default=-1,
+                    help="server launches in flight (1..16; -1: library default)")
     ap.add_argument("--serve-stream", type=int, choices=[-1, 0, 1], default=-1,
                     help="server kernel: 0 per-item barriers, 1 barrier-free, -1 library default")
     ap.add_argument("--serve-calib", type=int, default=256)
@@ -538,6 +544,12 @@ def run_serve(args):
     kw = {} if args.serve_stream < 0 else {"stream": args.serve_stream}
     if args.serve_steps_per_batch > 0:
         kw["steps_per_batch"] = args.serve_steps_per_batch
+    if args.serve_steps_per_item >= 0:
+        kw["steps_per_item"] = args.serve_steps_per_item
+    if args.serve_waves >= 0:
+        kw["waves"] = args.serve_waves
+    if args.serve_inflight_items >= 0:
+        kw["inflight_items"] = args.serve_inflight_items
     s = Server(slots=args.serve_slots, math=1 if args.math == "fast" else 0, **kw)
     # 1. calibration
     C = args.serve_calib
@@ -587,7 +599,9 @@ def run_serve(args):
         "config": {"workload": "served stream (config 4): Poisson arrivals, target RSE at shell 10 "
                                "in [0.5%, 5%], cap 2^24 photons, sweep parameter distribution",
                    "trace_seed": 0, "math": args.math, "slots": args.serve_slots,
-                   "kernel": kernel, "steps_per_batch": s.cfg.steps_per_batch},
+                   "kernel": kernel, "steps_per_batch": s.cfg.steps_per_batch,
+                   "steps_per_item": s.cfg.steps_per_item, "waves": s.cfg.waves or 16,
+                   "inflight_items": s.cfg.inflight_items},
         "latency_p50_s": pct(lat, 50), "latency_p99_s": pct(lat, 99),
         "photon_steps_per_s": steps3 / t_s,
         "requests": n3, "completed": int(done_s), "arrival_rate_per_s": rate,

@@ -299,6 +299,13 @@ typedef struct tmc_server_config {
     uint32_t max_items_per_request; /* RSE batches of one request in one wave */
     uint32_t stream;                /* 1: barrier-free kernel (up to two items open per block) */
     double steps_per_batch;         /* target photon steps per RSE batch */
+    double steps_per_item;          /* target photon steps per work item: a batch is split
+                                       into 2^k items walked by different blocks (0 = one
+                                       item per batch); results do not depend on it */
+    uint32_t waves;                 /* launches in flight at once, 1..16 (0 = 16) */
+    uint32_t inflight_items;        /* work items launched and not yet finished: no new
+                                       items above it, so new requests do not queue behind
+                                       long-running ones (0 = unbounded) */
 } tmc_server_config;
 
 typedef struct tmc_server tmc_server;

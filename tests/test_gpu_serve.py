@@ -73,6 +73,26 @@ def test_result_equals_plain_kernel_and_rule(tmc_mod, stream):
         assert b == cap_b or (b >= 16 and (b & (b - 1)) == 0)
 
 
+@pytest.mark.parametrize("stream", [0, 1])
+def test_item_split_does_not_change_results(tmc_mod, stream):
+    """RSE batches split into several work items (walked by different blocks),
+    fewer launches in flight and a small in-flight item budget give the same
+    tallies, steps, batch counts and RSE to the last bit."""
+    from tiny_mc_gb300.serve import Server
+    out = []
+    for spi, waves, items in ((0.0, 0, 0), (float(1 << 16), 4, 64)):
+        s = Server(slots=8, stream=stream, steps_per_item=spi, waves=waves, inflight_items=items)
+        ids = {s.submit(r): int(r["shells"]) for r in MIX}
+        out.append(s.run(ids))
+        s.close()
+    assert sorted(out[0]) == sorted(out[1])     # ids 1..5 in submit order on both servers
+    for rid in out[0]:
+        (ta, xa), (tb, xb) = out[0][rid], out[1][rid]
+        assert np.array_equal(ta, tb)
+        for f in ("photons", "photon_steps", "batches", "batch_photons", "reached_target", "rse"):
+            assert xa[f] == xb[f], f
+
+
 def test_admission_refuses_when_full(tmc_mod):
     from tiny_mc_gb300.serve import Server
     s = Server(slots=2)
@@ -100,8 +120,8 @@ def test_run_trace_small(tmc_mod):
     s.close()
 
 
-@pytest.mark.parametrize("stream", [0, 1])
-def test_rse_from_exact_batch_probes_with_wraps(tmc_mod, stream):
+@pytest.mark.parametrize("stream,spi", [(0, 0.0), (1, 0.0), (0, float(1 << 24)), (1, float(1 << 22))])
+def test_rse_from_exact_batch_probes_with_wraps(tmc_mod, stream, spi):
     """One shell and albedo 0.9999 with 2048-photon batches: each batch's sum
     of w in the probe shell (~2e7 weight units) exceeds 2^64 fixed-point
     units, so the per-item probe must count its wraps.  The server's RSE must
@@ -109,7 +129,7 @@ def test_rse_from_exact_batch_probes_with_wraps(tmc_mod, stream):
     plain-kernel tallies of the same photons."""
     from tiny_mc_gb300.serve import Server
     r = req(mu_a=0.1, mu_s=1000.0, shells=1, rse=1e-9, cap=32 * 2048, base=77 << 32)
-    s = Server(slots=4, steps_per_batch=float(1 << 28), stream=stream)
+    s = Server(slots=4, steps_per_batch=float(1 << 28), stream=stream, steps_per_item=spi)
     rid = s.submit(r)
     tally, res = s.run({rid: 1})[rid]
     s.close()

@@ -62,21 +62,27 @@ __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
         src.first = pr.id_base + item.first;
         unsigned long long *g = a.tally + 4 * pr.tally_offset;
         const uint32_t ps = min(a.probe_shell, S - 1);
+        const bool probe = a.item_probe || a.done_ring;
         const uint32_t steps = walk_loop<BLOCK, M>(pr.c, src, a.keys, smem, g, my,
-                                                   a.item_probe ? &sh_probe_wraps : nullptr, ps);
+                                                   probe ? &sh_probe_wraps : nullptr, ps);
 
         __syncthreads();
         flush_tally<BLOCK>(smem, S, g);
+        // this item's own sum of w in the probe shell, 128-bit: the block's
+        // 64-bit shared sum plus its counted 2^64 wraps
+        const unsigned long long probe_lo = ((unsigned long long)smem[S + ps] << 32) | smem[ps];
         if (a.item_probe && threadIdx.x == 0) {
-            // this item's own sum of w in the probe shell, 128-bit: the
-            // block's 64-bit shared sum plus its counted 2^64 wraps
-            a.item_probe[2 * (size_t)it] = ((unsigned long long)smem[S + ps] << 32) | smem[ps];
+            a.item_probe[2 * (size_t)it] = probe_lo;
             a.item_probe[2 * (size_t)it + 1] = sh_probe_wraps;
         }
         const unsigned long long tot = warp_sum_u64(steps);
         if ((threadIdx.x & 31u) == 0 && tot)
             atomicAdd(&a.steps[item.problem], tot);
+        if (a.done_ring)
+            __threadfence();
         __syncthreads();
+        if (a.done_ring && threadIdx.x == 0)
+            publish_item(a, it, probe_lo, sh_probe_wraps);
     }
 }
 
@@ -306,6 +312,8 @@ cudaError_t enqueue(const tmc_batch *b, cudaStream_t s)
     a.item_counter = b->d_counter;
     a.item_probe = nullptr;
     a.error = reinterpret_cast<unsigned *>(b->d_counter + 1);
+    a.done_ring = nullptr;
+    a.done_tail = nullptr;
     if (b->cfg.stream) {
         // two items open per block: no more blocks than half the items
         const int grid = std::max(1, std::min<int>(b->grid, (int)b->n_items));

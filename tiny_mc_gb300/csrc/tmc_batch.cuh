@@ -35,7 +35,30 @@ struct BatchArgs {
     unsigned long long *item_counter;  // zero at launch
     unsigned long long *item_probe;    // [n_items][2] (128-bit, lo then hi) or null
     unsigned *error;                   // walk_stream: set to 1 when a bounded wait ran out
+    // Completion ring or null: [n_items][4] in mapped host memory.  Each
+    // finished item takes the next entry (done_tail, zero at launch) and
+    // writes its probe value (lo, hi), its index, then 1 into the entry's
+    // last word, so the host can take items as they finish.
+    unsigned long long *done_ring;
+    unsigned *done_tail;
 };
+
+// Publish a finished item into the completion ring (one thread).  The
+// caller's block (or warp) has flushed the item's tally and added its steps,
+// each thread then fenced at device scope and synchronised with the caller:
+// the system-scope fence here orders all of that before the entry's ready
+// word, which the host reads with acquire semantics.
+__device__ __forceinline__ void publish_item(const BatchArgs &a, uint32_t it, unsigned long long lo,
+                                             unsigned long long hi)
+{
+    const unsigned slot = atomicAdd(a.done_tail, 1u);
+    volatile unsigned long long *e = a.done_ring + 4 * (size_t)slot;
+    e[0] = lo;
+    e[1] = hi;
+    e[2] = it;
+    __threadfence_system();
+    e[3] = 1ull;
+}
 
 size_t walk_batch_smem(uint32_t max_shells, int block);
 // Sets the kernel's shared-memory limit and returns the resident grid.

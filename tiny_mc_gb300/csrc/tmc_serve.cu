@@ -10,24 +10,26 @@
 //    queues; the tally and RNG state never leave the device while it runs;
 //  * walks a request in RSE batches of B photons (B a power of two chosen so
 //    one batch is about `steps_per_batch` photon steps, at least two photons
-//    per thread of a block).  A batch is one work item of the batched kernel,
-//    walked by one block, which also writes the item's own 128-bit sum of w
-//    in the probe shell;
+//    per thread of a block).  A batch is one or more work items (consecutive
+//    photon ranges, `steps_per_item`) of the batched kernel, each walked by one
+//    block, which also reports the item's own 128-bit sum of w in the probe
+//    shell;
 //  * stops a request only at fixed batch counts (min_batches, then doubling):
 //    there it computes the batch-means RSE of the probe shell in FP64 over
-//    batches 0..k-1 in order, and stops if RSE <= target or the cap is
-//    reached.  The decision depends only on the request's own photons, so a
-//    request's result is the same alone and in any mix;
-//  * runs work in waves: launches of the batched kernel over a bounded
-//    number of pending items, taken round-robin from the active requests,
-//    with up to sixteen waves in flight on sixteen streams (a wave finishes
-//    with its slowest item, so many in flight keep the SMs fed past the
-//    stragglers).  Requests that arrive
-//    while waves run are admitted and their items join the next wave while
-//    earlier ones are still on the device; a request's items may be spread
-//    over several waves, and its stop decision waits until every item before
-//    the decision point is back.  Batch values are summed from per-item
-//    values in item order, so the decision does not depend on timing.
+//    batches 0..k-1 in order (a batch's value is the exact integer sum of its
+//    items'), and stops if RSE <= target or the cap is reached.  The decision
+//    depends only on the request's own photons, so a request's result is the
+//    same alone, in any mix and under any of the scheduling settings;
+//  * runs work in waves: launches of the batched kernel over pending items,
+//    taken least-attained-service first (requests with the fewest photon
+//    steps issued so far go first, so a new request's first round does not
+//    queue behind the large later rounds of long-running ones), with up to
+//    `waves` (16) launches in flight on their own streams and optionally at
+//    most `inflight_items` items launched and unfinished;
+//  * takes each item as soon as it finishes: the kernel appends the item's
+//    probe value to a completion ring in mapped host memory after a
+//    system-scope fence, so a request's decision waits for its own items, not
+//    for the slowest item of the launch they were in.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -61,6 +63,7 @@ struct Req {
     uint32_t batch = 0;             // photons per RSE batch
     uint32_t item_photons = 0;      // photons per work item
     uint32_t items_per_batch = 0;
+    double est_steps = 0.0;         // expected photon steps per photon
     uint64_t max_batches = 0;
     uint64_t issued = 0, done = 0;  // work items
     uint64_t next_decision = 0;     // in batches
@@ -73,12 +76,13 @@ struct Wave {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     BatchItemDev *d_items = nullptr;
-    unsigned long long *d_probe = nullptr;
-    unsigned long long *d_counter = nullptr;
-    BatchItemDev *h_items = nullptr;        // pinned
-    unsigned long long *h_probe = nullptr;  // pinned
-    unsigned long long *h_err = nullptr;    // pinned: the wave's error flag
+    unsigned long long *d_counter = nullptr;   // item counter, error flag, ring tail
+    BatchItemDev *h_items = nullptr;           // pinned
+    unsigned long long *h_ring = nullptr;      // mapped: completion ring [items][4]
+    unsigned long long *d_ring = nullptr;      // its device address
+    unsigned long long *h_err = nullptr;       // pinned: the wave's error flag
     uint32_t n_items = 0;
+    uint32_t head = 0;                         // ring entries taken
     bool busy = false;
 };
 
@@ -102,8 +106,8 @@ struct tmc_server {
     std::unordered_map<uint64_t, Req> active;
     std::deque<uint64_t> order;              // admission order of active requests
     std::vector<uint64_t> slot_req;          // slot -> request id
-    size_t rr = 0;                           // round-robin cursor into order
     uint32_t wave_cap = 0;                   // items per wave
+    uint64_t inflight = 0;                   // work items launched, not harvested
     std::unordered_map<uint64_t, Done> finished;
     uint64_t next_id = 1;
     uint64_t photons = 0, steps = 0, n_waves = 0;
@@ -124,10 +128,9 @@ void destroy_server(tmc_server *s)
         if (w.stream)
             cudaStreamDestroy(w.stream);
         cudaFree(w.d_items);
-        cudaFree(w.d_probe);
         cudaFree(w.d_counter);
         cudaFreeHost(w.h_items);
-        cudaFreeHost(w.h_probe);
+        cudaFreeHost(w.h_ring);
         cudaFreeHost(w.h_err);
     }
     if (s->admin)
@@ -152,6 +155,22 @@ uint32_t batch_photons(const tmc_server_config &cfg, double est_steps)
     return b;
 }
 
+// Work items per RSE batch: a power of two (batch is one too) so that an item
+// is about steps_per_item photon steps, but no smaller than the kernel's
+// smallest item (batch_photons' lower bound).  A batch's items are
+// consecutive photon ranges walked by different blocks at once, so a decision
+// round takes the time of one item, not of one batch; the batch's probe value
+// is the exact sum of its items', so results do not depend on the split.
+uint32_t items_per_batch(const tmc_server_config &cfg, uint32_t batch, double est_steps)
+{
+    const uint32_t lo = cfg.stream ? (uint32_t)BATCH_CHUNK : 2 * cfg.block;
+    uint32_t k = 1;
+    if (cfg.steps_per_item > 0.0)
+        while (batch / (2 * k) >= lo && (double)(batch / k) * est_steps > 2.0 * cfg.steps_per_item)
+            k *= 2;
+    return k;
+}
+
 double expected_steps_host(float albedo)
 {
     if (!(albedo > 0.0f))
@@ -172,12 +191,18 @@ double expected_steps_host(float albedo)
 double batch_rse(const std::vector<unsigned long long> &probe, uint32_t ipb, uint64_t k,
                  double *mean_out)
 {
+    // a batch's value: the exact 128-bit sum of its items' probes (64-bit sum
+    // plus counted 2^64 wraps), converted to weight units once, so it does not
+    // depend on how many items the batch was split into
     std::vector<double> x(k, 0.0);
-    for (uint64_t j = 0; j < k; ++j)
+    for (uint64_t j = 0; j < k; ++j) {
+        unsigned __int128 v = 0;
         for (uint32_t i = 0; i < ipb; ++i) {
             const uint64_t g = j * ipb + i;
-            x[j] += (double)probe[2 * g + 1] * 0x1p24 + (double)probe[2 * g] * 0x1p-40;
+            v += ((unsigned __int128)probe[2 * g + 1] << 64) + probe[2 * g];
         }
+        x[j] = (double)(unsigned long long)(v >> 64) * 0x1p24 + (double)(unsigned long long)v * 0x1p-40;
+    }
     double sum = 0.0;
     for (uint64_t j = 0; j < k; ++j)
         sum += x[j];
@@ -240,24 +265,36 @@ int decide(tmc_server *s, uint64_t id)
     return TMC_OK;
 }
 
-// Harvest a completed wave: store per-item values, decide where possible.
-int harvest(tmc_server *s, Wave &w)
+// Take the items of a wave that have finished (its completion ring, in
+// finishing order), store their probe values and decide where possible.
+// ended: the wave's launch and its error-flag copy are complete, so every
+// item is in the ring unless a bounded device wait ran out.
+int harvest(tmc_server *s, Wave &w, bool ended)
 {
-    if (*w.h_err) {
+    if (ended && *w.h_err) {
         set_error_text("server wave: a bounded device wait ran out");
         return TMC_E_TIMEOUT;
     }
     std::vector<uint64_t> touched;
-    for (uint32_t i = 0; i < w.n_items; ++i) {
+    while (w.head < w.n_items) {
+        unsigned long long *e = w.h_ring + 4 * (size_t)w.head;
+        if (__atomic_load_n(&e[3], __ATOMIC_ACQUIRE) == 0)
+            break;
+        const uint64_t i = e[2];
+        if (i >= w.n_items) {
+            set_error_text("server wave: bad completion-ring entry");
+            return TMC_E_STATE;
+        }
         const BatchItemDev &it = w.h_items[i];
         const uint64_t id = s->slot_req[it.problem];
         Req &q = s->active[id];
         const uint64_t g = it.first / q.item_photons;
-        q.probe[2 * g] = w.h_probe[2 * (size_t)i];
-        q.probe[2 * g + 1] = w.h_probe[2 * (size_t)i + 1];
+        q.probe[2 * g] = e[0];
+        q.probe[2 * g + 1] = e[1];
         ++q.done;
-        if (touched.empty() || touched.back() != id)
-            touched.push_back(id);
+        --s->inflight;
+        touched.push_back(id);
+        ++w.head;
     }
     std::sort(touched.begin(), touched.end());
     touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
@@ -266,8 +303,14 @@ int harvest(tmc_server *s, Wave &w)
         if (st)
             return st;
     }
-    w.busy = false;
-    w.n_items = 0;
+    if (ended) {
+        if (w.head != w.n_items) {
+            set_error_text("server wave: finished items missing from the completion ring");
+            return TMC_E_STATE;
+        }
+        w.busy = false;
+        w.n_items = 0;
+    }
     return TMC_OK;
 }
 
@@ -285,14 +328,27 @@ int launch_wave(tmc_server *s, Wave &w)
         return TMC_OK;
     const uint64_t quota = std::max<uint64_t>(
         16, std::min<uint64_t>(s->cfg.max_items_per_request, s->wave_cap / pending_reqs));
-    const size_t m = s->order.size();
-    for (size_t c = 0; c < m && n < s->wave_cap; ++c) {
-        const uint64_t id = s->order[(s->rr + c) % m];
+    // least attained service first: requests with the fewest photon steps
+    // issued so far (new requests' first rounds) go ahead of the later, larger
+    // rounds of long-running ones; ties in admission order
+    std::vector<std::pair<double, uint64_t>> pend;
+    pend.reserve(pending_reqs);
+    for (uint64_t id : s->order) {
+        const Req &q = s->active[id];
+        if (q.issued < q.next_decision * q.items_per_batch)
+            pend.push_back({(double)q.issued * q.item_photons * q.est_steps, id});
+    }
+    std::stable_sort(pend.begin(), pend.end(),
+                     [](const auto &x, const auto &y) { return x.first < y.first; });
+    const uint64_t room = s->cfg.inflight_items
+                              ? (s->inflight < s->cfg.inflight_items ? s->cfg.inflight_items - s->inflight : 0)
+                              : ~0ull;
+    const uint64_t cap_n = std::min<uint64_t>(s->wave_cap, room);
+    for (size_t c = 0; c < pend.size() && n < cap_n; ++c) {
+        const uint64_t id = pend[c].second;
         Req &q = s->active[id];
         const uint64_t limit = q.next_decision * q.items_per_batch;
-        if (q.issued >= limit)
-            continue;
-        const uint64_t k = std::min<uint64_t>({limit - q.issued, quota, (uint64_t)(s->wave_cap - n)});
+        const uint64_t k = std::min<uint64_t>({limit - q.issued, quota, cap_n - n});
         for (uint64_t j = 0; j < k; ++j) {
             BatchItemDev &it = w.h_items[n++];
             it.problem = (uint32_t)q.slot;
@@ -303,14 +359,16 @@ int launch_wave(tmc_server *s, Wave &w)
         if (q.probe.size() < 2 * q.issued)
             q.probe.resize(2 * q.issued, 0ull);
     }
-    s->rr = m ? (s->rr + 1) % m : 0;
     if (n == 0)
         return TMC_OK;
     w.n_items = n;
+    w.head = 0;
+    s->inflight += n;
+    std::memset(w.h_ring, 0, 4 * sizeof(unsigned long long) * n);   // the wave is idle
     cudaError_t e = cudaMemcpyAsync(w.d_items, w.h_items, sizeof(BatchItemDev) * n,
                                     cudaMemcpyHostToDevice, w.stream);
-    if (e == cudaSuccess)   // item counter and error flag
-        e = cudaMemsetAsync(w.d_counter, 0, 2 * sizeof(unsigned long long), w.stream);
+    if (e == cudaSuccess)   // item counter, error flag, ring tail
+        e = cudaMemsetAsync(w.d_counter, 0, 3 * sizeof(unsigned long long), w.stream);
     if (e == cudaSuccess) {
         BatchArgs a;
         a.keys = s->keys;
@@ -322,8 +380,10 @@ int launch_wave(tmc_server *s, Wave &w)
         a.tally = s->d_tally;
         a.steps = s->d_steps;
         a.item_counter = w.d_counter;
-        a.item_probe = w.d_probe;
+        a.item_probe = nullptr;
         a.error = reinterpret_cast<unsigned *>(w.d_counter + 1);
+        a.done_ring = w.d_ring;
+        a.done_tail = reinterpret_cast<unsigned *>(w.d_counter + 2);
         if (s->cfg.stream)
             e = walk_stream_launch(a, (int)s->cfg.block, s->cfg.math,
                                    std::max(1, std::min<int>(s->grid, (int)n)), w.stream);
@@ -334,9 +394,6 @@ int launch_wave(tmc_server *s, Wave &w)
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(w.h_err, w.d_counter + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                             w.stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(w.h_probe, w.d_probe, 2 * sizeof(unsigned long long) * n,
-                            cudaMemcpyDeviceToHost, w.stream);
     if (e == cudaSuccess)
         e = cudaEventRecord(w.done, w.stream);
     if (e != cudaSuccess)
@@ -351,21 +408,26 @@ int progress_locked(tmc_server *s)
     for (Wave &w : s->waves) {
         if (!w.busy)
             continue;
-        cudaError_t e = cudaEventQuery(w.done);
-        if (e == cudaErrorNotReady)
-            continue;
-        if (e != cudaSuccess)
+        const cudaError_t e = cudaEventQuery(w.done);
+        if (e != cudaSuccess && e != cudaErrorNotReady)
             return set_cuda_error(e, "server wave");
-        int st = harvest(s, w);
+        int st = harvest(s, w, e == cudaSuccess);
         if (st)
             return st;
     }
+    const uint32_t cap = s->cfg.waves ? s->cfg.waves : (uint32_t)WAVES;
+    uint32_t busy = 0;
+    for (const Wave &w : s->waves)
+        busy += w.busy ? 1u : 0u;
     for (Wave &w : s->waves) {
+        if (busy >= cap || (s->cfg.inflight_items && s->inflight >= s->cfg.inflight_items))
+            break;
         if (w.busy)
             continue;
         int st = launch_wave(s, w);
         if (st)
             return st;
+        busy += w.busy ? 1u : 0u;
     }
     return TMC_OK;
 }
@@ -397,7 +459,8 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
     *out = nullptr;
     if (cfg->slots == 0 || cfg->slots > (1u << 20) || cfg->max_shells == 0 ||
         cfg->max_shells > (1u << 16) || cfg->min_batches < 2 || cfg->max_items_per_request == 0 ||
-        !(cfg->steps_per_batch > 0.0) || (cfg->math != TMC_MATH_EXACT && cfg->math != TMC_MATH_FAST) ||
+        !(cfg->steps_per_batch > 0.0) || !(cfg->steps_per_item >= 0.0) || cfg->waves > (uint32_t)WAVES ||
+        (cfg->math != TMC_MATH_EXACT && cfg->math != TMC_MATH_FAST) ||
         (cfg->block != 128 && cfg->block != 256 && cfg->block != 512))
         return TMC_E_INVALID;
     std::lock_guard<std::mutex> lk(api_mutex());
@@ -439,15 +502,15 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
         if (e == cudaSuccess)
             e = cudaMalloc(&w.d_items, sizeof(BatchItemDev) * s->items_cap);
         if (e == cudaSuccess)
-            e = cudaMalloc(&w.d_probe, 2 * sizeof(unsigned long long) * s->items_cap);
-        if (e == cudaSuccess)
-            e = cudaMalloc(&w.d_counter, 2 * sizeof(unsigned long long));
+            e = cudaMalloc(&w.d_counter, 3 * sizeof(unsigned long long));
         if (e == cudaSuccess)
             e = cudaMallocHost(&w.h_err, sizeof(unsigned long long));
         if (e == cudaSuccess)
             e = cudaMallocHost(&w.h_items, sizeof(BatchItemDev) * s->items_cap);
         if (e == cudaSuccess)
-            e = cudaMallocHost(&w.h_probe, 2 * sizeof(unsigned long long) * s->items_cap);
+            e = cudaHostAlloc(&w.h_ring, 4 * sizeof(unsigned long long) * s->items_cap, cudaHostAllocMapped);
+        if (e == cudaSuccess)
+            e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&w.d_ring), w.h_ring, 0);
     }
     if (e != cudaSuccess)
         return set_cuda_error(e, "tmc_server_create");
@@ -480,9 +543,11 @@ int tmc_server_submit(tmc_server *s, const tmc_request *r, uint64_t *id)
     q.id = s->next_id++;
     q.r = *r;
     q.d = derive(r->mu_a, r->mu_s, r->microns_per_shell, r->shells);
-    q.batch = batch_photons(s->cfg, expected_steps_host(q.d.albedo));
-    q.item_photons = q.batch;
-    q.items_per_batch = 1;
+    const double est = expected_steps_host(q.d.albedo);
+    q.est_steps = est;
+    q.batch = batch_photons(s->cfg, est);
+    q.items_per_batch = items_per_batch(s->cfg, q.batch, est);
+    q.item_photons = q.batch / q.items_per_batch;
     q.max_batches = std::max<uint64_t>(1, (r->max_photons + q.batch - 1) / q.batch);
     q.next_decision = std::min<uint64_t>(s->cfg.min_batches, q.max_batches);
     q.slot = s->free_slots.back();

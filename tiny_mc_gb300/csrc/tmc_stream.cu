@@ -152,17 +152,24 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
                     flush128(&gg[4 * s + 2], &gg[4 * s + 3],
                              ((unsigned long long)hist[3 * S + s] << 32) | hist[2 * S + s]);
                 }
+                const uint32_t p = vopen[rb].ps;
+                const unsigned long long probe_lo = ((unsigned long long)hist[S + p] << 32) | hist[p];
+                const unsigned long long probe_hi = vopen[rb].wraps;
                 if (lane == 0) {
                     const unsigned long long st =
                         ((unsigned long long)vopen[rb].steps_hi << 32) | vopen[rb].steps_lo;
                     if (st)
                         atomicAdd(&a.steps[a.items[it].problem], st);
                     if (a.item_probe) {
-                        const uint32_t p = vopen[rb].ps;
-                        a.item_probe[2 * (size_t)it] =
-                            ((unsigned long long)hist[S + p] << 32) | hist[p];
-                        a.item_probe[2 * (size_t)it + 1] = vopen[rb].wraps;
+                        a.item_probe[2 * (size_t)it] = probe_lo;
+                        a.item_probe[2 * (size_t)it + 1] = probe_hi;
                     }
+                }
+                if (a.done_ring) {
+                    __threadfence();
+                    __syncwarp();
+                    if (lane == 0)
+                        publish_item(a, it, probe_lo, probe_hi);
                 }
                 __syncwarp();
                 for (uint32_t s = lane; s < 4 * S; s += 32)
