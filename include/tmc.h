@@ -302,7 +302,7 @@ typedef struct tmc_server_config {
     double steps_per_item;          /* target photon steps per work item: a batch is split
                                        into 2^k items walked by different blocks (0 = one
                                        item per batch); results do not depend on it */
-    uint32_t waves;                 /* launches in flight at once, 1..16 (0 = 16) */
+    uint32_t waves;                 /* launches in flight at once, 1..64 (0 = 16) */
     uint32_t inflight_items;        /* work items launched and not yet finished: no new
                                        items above it, so new requests do not queue behind
                                        long-running ones (0 = unbounded) */

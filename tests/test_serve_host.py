@@ -19,7 +19,7 @@ def test_trace_shape_and_rates():
 
 @pytest.mark.parametrize("field,value", [("slots", 0), ("max_shells", 0), ("min_batches", 1),
                                          ("block", 100), ("math", 9), ("max_items_per_request", 0),
-                                         ("waves", 17), ("steps_per_item", -1.0),
+                                         ("waves", 65), ("steps_per_item", -1.0),
                                          ("steps_per_batch", 0.0)])
 def test_invalid_server_config_rejected(tmc_mod, field, value):
     from tiny_mc_gb300.serve import default_config

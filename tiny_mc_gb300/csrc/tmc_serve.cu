@@ -24,7 +24,7 @@
 //    taken least-attained-service first (requests with the fewest photon
 //    steps issued so far go first, so a new request's first round does not
 //    queue behind the large later rounds of long-running ones), with up to
-//    `waves` (16) launches in flight on their own streams and optionally at
+//    `waves` (16, at most 64) launches in flight on their own streams and at
 //    most `inflight_items` items launched and unfinished;
 //  * takes each item as soon as it finishes: the kernel appends the item's
 //    probe value to a completion ring in mapped host memory after a
@@ -47,7 +47,8 @@ using namespace tmc;
 
 namespace {
 
-constexpr int WAVES = 16;
+constexpr int WAVES = 64;           // launch slots (streams, buffers)
+constexpr uint32_t DEFAULT_WAVES = 16;
 using Clock = std::chrono::steady_clock;
 
 double now_s()
@@ -415,7 +416,7 @@ int progress_locked(tmc_server *s)
         if (st)
             return st;
     }
-    const uint32_t cap = s->cfg.waves ? s->cfg.waves : (uint32_t)WAVES;
+    const uint32_t cap = s->cfg.waves ? s->cfg.waves : DEFAULT_WAVES;
     uint32_t busy = 0;
     for (const Wave &w : s->waves)
         busy += w.busy ? 1u : 0u;
