@@ -13,7 +13,7 @@ one JSON line (rank 0).  Usage:
 * e2e: the same metric through the C ABI's host-array call
   tmc_photon_batch(heat, heat2, n, params), wall time of the whole call
   (launch, walk, FP64 finalisation, device-to-host copy of the result);
-* roofline: the benchmark spec's bound of this path, SFU-class operations
+* roofline: the bound named for this path, SFU-class operations
   (4 per photon step: log, 2 sqrt, divide) against the measured MUFU rate;
 * cpu_baseline: the reference's walk on this host's cores (libc rand).
 
@@ -38,7 +38,7 @@ METRIC = "photons/s on 1 GB300 (plain vs batched/served) at stated error; p50/p9
 UNIT = "photons/s"
 SFU_OPS_PER_STEP = 4          # log, sqrt (radius), divide + sqrt (direction)
 CPU_PHOTONS_PER_PROC = 1 << 16
-# Issue-slot accounting of walk_plain<256, FastMath> at config-1 optics, from
+# Issue-slot accounting of walk_plain<256, FastMath> at params.h optics, from
 # ncu --set full of one 2^25-photon launch (profiles/walk_plain_fast_
 # 2p25photons_ncu_full.txt): thread-instructions per photon step and the busy
 # fraction of each pipe.  An SM issues at most 4 warp-instructions per clock.
@@ -46,7 +46,7 @@ WALK_THREAD_INSTR_PER_STEP = 229.6
 WALK_PIPES_NCU = {"issue_slots": 0.796, "alu": 0.543, "fma_heavy": 0.522, "xu_sfu": 0.199,
                   "shared_wavefronts": 0.504, "dram": 0.0}
 # DRAM bytes (read + write) of one walk launch, from an ncu capture of the walk
-# at config-1 optics (2^25 photons): only the 101-shell tally flush touches
+# at params.h optics (2^25 photons): only the 101-shell tally flush touches
 # DRAM, so the figure does not grow with the photon count.
 WALK_DRAM_BYTES_PER_LAUNCH = 19968
 
@@ -63,13 +63,13 @@ def parse():
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--optics", choices=["cfg1", "cfg2"], default="cfg1",
-                    help="plain workload optics: cfg1 = params.h (101 shells, 50 um, MU_A 2, MU_S 20); "
-                         "cfg2 = high albedo (1001 shells, 10 um, MU_A 0.1, MU_S 100)")
+    ap.add_argument("--optics", choices=["params_h", "high_albedo"], default="params_h",
+                    help="plain workload optics: params_h = params.h (101 shells, 50 um, MU_A 2, MU_S 20); "
+                         "high_albedo = high albedo (1001 shells, 10 um, MU_A 0.1, MU_S 100)")
     ap.add_argument("--sweep-mu-a-min", type=float, default=0.01,
-                    help="sweep workload: lower end of the mu_a range (0.01 = config 3)")
+                    help="sweep workload: lower end of the mu_a range (0.01: the full sweep distribution)")
     ap.add_argument("--workload", choices=["plain", "sweep", "serve"], default="plain",
-                    help="plain: config 1 (default); sweep: the 4096-problem batched sweep; "
+                    help="plain: 2^30 photons at params.h optics (default); sweep: the 4096-problem batched sweep; "
                          "serve: the request stream")
     ap.add_argument("--serve-slots", type=int, default=1024)
     ap.add_argument("--serve-steps-per-batch", type=float, default=0.0,
@@ -95,13 +95,13 @@ def parse():
     return ap.parse_args()
 
 
-OPTICS = {"cfg1": dict(shells=101, microns_per_shell=50.0, mu_a=2.0, mu_s=20.0),
-          "cfg2": dict(shells=1001, microns_per_shell=10.0, mu_a=0.1, mu_s=100.0)}
+OPTICS = {"params_h": dict(shells=101, microns_per_shell=50.0, mu_a=2.0, mu_s=20.0),
+          "high_albedo": dict(shells=1001, microns_per_shell=10.0, mu_a=0.1, mu_s=100.0)}
 
 
 def workload_config(args, world):
     o = OPTICS[args.optics]
-    name = ("plain walk, 2^30 photons per GPU (config 1)" if args.optics == "cfg1" and
+    name = ("plain walk, 2^30 photons per GPU, params.h optics" if args.optics == "params_h" and
             args.photons == 1 << 30 else f"plain walk, {args.photons} photons per GPU ({args.optics} optics)")
     return {
         "workload": name,
@@ -122,13 +122,13 @@ def _cpu_worker(args):
     photons, seed = args
     sys.path.insert(0, ROOT)
     from oracle import oracle
-    if oracle.ref_available("cfg0", "nat"):
+    if oracle.ref_available("params_h", "nat"):
         try:
-            L = oracle.ref_lib("cfg0", "nat")
+            L = oracle.ref_lib("params_h", "nat")
             return L.ref_native_rate(photons, seed), "reference"
         except OSError:
             pass
-    rate, _ = oracle.native_rate(oracle.cfg("cfg0"), photons, seed)
+    rate, _ = oracle.native_rate(oracle.cfg("params_h"), photons, seed)
     return rate, "port"
 
 
@@ -358,7 +358,7 @@ def run_ours(args):
     roofline = {
         "bound": "sfu", "achieved": achieved / 1e9, "peak": sfu_peak / 1e9, "unit": "Gop/s",
         "frac": achieved / sfu_peak,
-        "traffic": WALK_DRAM_BYTES_PER_LAUNCH if args.optics == "cfg1" else None,
+        "traffic": WALK_DRAM_BYTES_PER_LAUNCH if args.optics == "params_h" else None,
         "traffic_note": "DRAM bytes per launch (ncu, 101 shells); tally flush only, independent of photons",
         "algorithmic_unit": "4 SFU-class ops (log, sqrt, divide, sqrt) per photon step",
         "photon_steps_per_launch": photon_steps / args.steps,
@@ -367,7 +367,7 @@ def run_ours(args):
     # the pipe that binds: instruction issue (4 warp-instructions per clock per
     # SM); its ceiling at the sampled clock, and the ncu pipe utilisations
     mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
-    if mhz and args.optics == "cfg1" and args.math == "fast":
+    if mhz and args.optics == "params_h" and args.math == "fast":
         issue_steps = props.multi_processor_count * mhz * 1e6 * 4 * 32 / WALK_THREAD_INSTR_PER_STEP
         roofline["binding_pipe"] = {
             "pipe": "instruction issue", "thread_instr_per_step": WALK_THREAD_INSTR_PER_STEP,
@@ -432,7 +432,7 @@ def run_ours(args):
 
 
 def run_sweep(args):
-    """Config 3: 4096 independent problems (seeded draw of the sweep's
+    """The batched sweep: 4096 independent problems (seeded draw of the sweep's
     parameter distribution) in one persistent launch per step, against the
     plain form (one launch per problem, back to back on one stream)."""
     import torch
@@ -503,7 +503,7 @@ def run_sweep(args):
         "metric": METRIC, "value": batched, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sum(ms) / len(ms), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "batched sweep (config 3): 4096 problems in one persistent launch",
+        "config": {"workload": "batched sweep: 4096 problems in one persistent launch",
                    "photon_scale": args.sweep_scale, "photons_per_step": photons,
                    "photon_steps_per_step": photon_steps,
                    "est_photon_steps_per_step": est_steps, "math": args.math,
@@ -522,7 +522,7 @@ def run_sweep(args):
 
 
 def run_serve(args):
-    """Config 4: Poisson arrivals of requests with the sweep's parameter
+    """The served stream: Poisson arrivals of requests with the sweep's parameter
     distribution, a target RSE at shell 10 in [0.5 %, 5 %] and a 2^24-photon
     cap.  Three measurements on one server:
       1. calibration: the first requests of the trace submitted at once give
@@ -596,7 +596,7 @@ def run_serve(args):
         "metric": METRIC, "value": photons3 / t_s, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 0,
         "ms_per_step": t_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "served stream (config 4): Poisson arrivals, target RSE at shell 10 "
+        "config": {"workload": "served stream: Poisson arrivals, target RSE at shell 10 "
                                "in [0.5%, 5%], cap 2^24 photons, sweep parameter distribution",
                    "trace_seed": 0, "math": args.math, "slots": args.serve_slots,
                    "kernel": kernel, "steps_per_batch": s.cfg.steps_per_batch,

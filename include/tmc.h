@@ -53,7 +53,7 @@ typedef enum tmc_math {
     /* Hardware approximations: lg2.approx for the logarithm, sqrt.approx,
      * contracted multiply-adds and (1-u^2)/t rewritten as 4(1-t).  Same draws
      * and branch decisions; tallies agree with the exact form statistically
-     * (per-shell relative differences far below 1e-4 at config-1 optics). */
+     * (per-shell relative differences far below 1e-4 at params.h optics). */
     TMC_MATH_FAST = 1
 } tmc_math;
 

@@ -2,7 +2,8 @@
 builds in oracle/_ref/.
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
-by bench.py's CPU-baseline leg — as the checker, never as the product path.
+by bench.py's CPU-baseline leg — as the oracle results are compared against,
+never as the product path.
 
 What each call restates (reference = computacionparalela/tiny_mc):
   walk_fx, photon_hashes   photon.c:6-51 in FP32, photon.c's evaluation order
@@ -28,8 +29,8 @@ LOG_NATIVE = 1
 
 CONFIGS = {
     # name: (shells, microns_per_shell, mu_a, mu_s)
-    "cfg0": (101, 50.0, 2.0, 20.0),
-    "cfg2": (1001, 10.0, 0.1, 100.0),
+    "params_h": (101, 50.0, 2.0, 20.0),
+    "high_albedo": (1001, 10.0, 0.1, 100.0),
 }
 
 

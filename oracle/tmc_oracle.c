@@ -1,7 +1,7 @@
 /*
  * tmc_oracle.c — CPU oracle for the tiny_mc photon walk.
  *
- * TEST INFRASTRUCTURE ONLY (the checker, never the product): the product
+ * TEST INFRASTRUCTURE ONLY (the oracle, never the product): the product
  * library does not link, load or call anything in oracle/.
  *
  * Must be compiled with -std=c11 -ffp-contract=off (the Makefile does): the

@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links or calls
  * this code; the tests, the smoke check and the CPU-baseline leg of the bench
- * use it as the checker.
+ * compare against it.
  *
  * What it restates (reference = computacionparalela/tiny_mc):
  *   photon.c:6-51   the walk of one photon (launch, move, absorb, re-direct,

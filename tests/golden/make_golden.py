@@ -5,18 +5,19 @@ Needs the reference tree (computacionparalela/tiny_mc) — by default
 (the reference's own sources compiled unchanged, see oracle/Makefile) and
 records what those binaries print or compute:
 
-  ref_cfg0_seed1_stdout.txt   stdout of the reference's headless program at
+  ref_params_h_seed1_stdout.txt  stdout of the reference's headless program at
                               -DSEED=1, the two timing lines (8-9) removed
   ref_native.npz              the reference's float heat/heat2 arrays after
                               srand(1) and N photons (tiny_mc.c:43-49), and
                               per-batch arrays of consecutive photon groups
-                              (cfg0: 32768 photons = 32 x 1024; cfg2: 4096 =
-                              32 x 128), as raw float32
+                              (params_h: 32768 photons = 32 x 1024;
+                              high_albedo: 4096 = 32 x 128), as raw float32
   ref_injected.npz            per-photon FNV-1a hashes and summed float
                               arrays of the reference's photon() fed by the
                               oracle's Philox streams (seed 1), with the
                               oracle's logarithm (log0) and with libm logf
-                              (log1): cfg0 photons 0..511, cfg2 photons 0..31
+                              (log1): params_h photons 0..511, high_albedo
+                              photons 0..31
 
 Run:  python tests/golden/make_golden.py
 """
@@ -41,12 +42,12 @@ def main() -> None:
     out = subprocess.run([oracle.ref_binary()], capture_output=True, text=True, check=True).stdout
     lines = out.splitlines(keepends=True)
     del lines[7:9]
-    with open(os.path.join(HERE, "ref_cfg0_seed1_stdout.txt"), "w") as f:
+    with open(os.path.join(HERE, "ref_params_h_seed1_stdout.txt"), "w") as f:
         f.writelines(lines)
 
     # 2. native-RNG arrays and batches
     arrays = {}
-    for name, n, batch in (("cfg0", 32768, 1024), ("cfg2", 4096, 128)):
+    for name, n, batch in (("params_h", 32768, 1024), ("high_albedo", 4096, 128)):
         h, h2 = oracle.ref_native_run(name, n, 1)
         bh, bh2 = oracle.ref_native_batches(name, n, 1, batch)
         arrays[f"{name}_n"] = np.array(n)
@@ -59,7 +60,7 @@ def main() -> None:
 
     # 3. the reference's photon() on injected Philox streams
     inj = {}
-    for name, n in (("cfg0", 512), ("cfg2", 32)):
+    for name, n in (("params_h", 512), ("high_albedo", 32)):
         for log_mode in (oracle.LOG_TMC, oracle.LOG_NATIVE):
             hashes, hs, h2s = oracle.ref_photon_hashes(name, n, seed=1, log_mode=log_mode)
             inj[f"{name}_log{log_mode}_hashes"] = hashes

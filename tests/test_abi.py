@@ -84,9 +84,9 @@ def test_report_reproduces_reference_stdout(tmc_mod):
     """tmc_format_report on the reference's own float arrays (srand(1), 32768
     photons) prints byte-for-byte the table the reference printed."""
     g = np.load(os.path.join(GOLDEN, "ref_native.npz"))
-    golden = open(os.path.join(GOLDEN, "ref_cfg0_seed1_stdout.txt")).read().splitlines(keepends=True)
+    golden = open(os.path.join(GOLDEN, "ref_params_h_seed1_stdout.txt")).read().splitlines(keepends=True)
     p = tmc_mod.params()
-    table = tmc_mod.format_report(g["cfg0_heat"], g["cfg0_heat2"], 32768, p)
+    table = tmc_mod.format_report(g["params_h_heat"], g["params_h_heat2"], 32768, p)
     assert table == "".join(golden[7:])
 
 

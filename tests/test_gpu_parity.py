@@ -16,8 +16,8 @@ from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
-CFG0 = dict(shells=101, microns_per_shell=50.0, mu_a=2.0, mu_s=20.0)
-CFG2 = dict(shells=1001, microns_per_shell=10.0, mu_a=0.1, mu_s=100.0)
+PARAMS_H = dict(shells=101, microns_per_shell=50.0, mu_a=2.0, mu_s=20.0)
+HIGH_ALBEDO = dict(shells=1001, microns_per_shell=10.0, mu_a=0.1, mu_s=100.0)
 
 
 def as_array(tally):
@@ -49,17 +49,17 @@ def test_device_rand_stream_matches_oracle(tmc_mod, oracle_mod):
 
 
 @pytest.mark.parametrize("seed,base,n", [(1, 0, 1 << 16), (12345, 1 << 40, 50000)])
-def test_exact_bit_identical_cfg0(tmc_mod, oracle_mod, seed, base, n):
-    got, steps = gpu_fx(tmc_mod, n, seed=seed, base=base, **CFG0)
-    ref, dep, ref_steps = oracle_fx(oracle_mod, n, seed=seed, base=base, **CFG0)
+def test_exact_bit_identical_params_h(tmc_mod, oracle_mod, seed, base, n):
+    got, steps = gpu_fx(tmc_mod, n, seed=seed, base=base, **PARAMS_H)
+    ref, dep, ref_steps = oracle_fx(oracle_mod, n, seed=seed, base=base, **PARAMS_H)
     assert steps == ref_steps
     assert np.array_equal(got, ref)
 
 
-def test_exact_bit_identical_cfg2(tmc_mod, oracle_mod):
+def test_exact_bit_identical_high_albedo(tmc_mod, oracle_mod):
     n = 2048
-    got, steps = gpu_fx(tmc_mod, n, **CFG2)
-    ref, _, ref_steps = oracle_fx(oracle_mod, n, **CFG2)
+    got, steps = gpu_fx(tmc_mod, n, **HIGH_ALBEDO)
+    ref, _, ref_steps = oracle_fx(oracle_mod, n, **HIGH_ALBEDO)
     assert steps == ref_steps
     assert np.array_equal(got, ref)
 
@@ -96,24 +96,24 @@ def test_exact_bit_identical_wide_tallies(tmc_mod, oracle_mod, shells, mps, n, n
 
 @pytest.mark.parametrize("n", [0, 1, 31, 32, 33, 255, 257, 4097])
 def test_edge_photon_counts(tmc_mod, oracle_mod, n):
-    got, steps = gpu_fx(tmc_mod, n, seed=3, **CFG0)
-    ref, _, ref_steps = oracle_fx(oracle_mod, n, seed=3, **CFG0)
+    got, steps = gpu_fx(tmc_mod, n, seed=3, **PARAMS_H)
+    ref, _, ref_steps = oracle_fx(oracle_mod, n, seed=3, **PARAMS_H)
     assert steps == ref_steps
     assert np.array_equal(got, ref)
 
 
 @pytest.mark.parametrize("block,bpsm,maxb", [(128, 0, 0), (256, 1, 0), (512, 0, 0), (512, 1, 3), (128, 2, 1)])
 def test_launch_shape_invariance(tmc_mod, block, bpsm, maxb):
-    base, _ = gpu_fx(tmc_mod, 40000, seed=11, **CFG0)
+    base, _ = gpu_fx(tmc_mod, 40000, seed=11, **PARAMS_H)
     tmc_mod.set_plain_launch(block, bpsm, maxb)
-    got, _ = gpu_fx(tmc_mod, 40000, seed=11, **CFG0)
+    got, _ = gpu_fx(tmc_mod, 40000, seed=11, **PARAMS_H)
     assert np.array_equal(got, base)
 
 
 def test_split_ranges_add_up(tmc_mod):
-    whole, s0 = gpu_fx(tmc_mod, 30000, seed=5, **CFG0)
-    a, s1 = gpu_fx(tmc_mod, 12345, seed=5, base=0, **CFG0)
-    b, s2 = gpu_fx(tmc_mod, 30000 - 12345, seed=5, base=12345, **CFG0)
+    whole, s0 = gpu_fx(tmc_mod, 30000, seed=5, **PARAMS_H)
+    a, s1 = gpu_fx(tmc_mod, 12345, seed=5, base=0, **PARAMS_H)
+    b, s2 = gpu_fx(tmc_mod, 30000 - 12345, seed=5, base=12345, **PARAMS_H)
     tot = [(int(a[i, 1]) << 64 | int(a[i, 0])) + (int(b[i, 1]) << 64 | int(b[i, 0])) for i in range(101)]
     assert tot == [int(whole[i, 1]) << 64 | int(whole[i, 0]) for i in range(101)]
     assert s1 + s2 == s0
@@ -135,45 +135,45 @@ def test_carry_paths_128bit(tmc_mod, oracle_mod):
 
 
 def test_photon_batch_float_accumulates(tmc_mod, oracle_mod):
-    p = tmc_mod.params(seed=2, **CFG0)
+    p = tmc_mod.params(seed=2, **PARAMS_H)
     heat = np.zeros(101, np.float32)
     heat2 = np.zeros(101, np.float32)
     tmc_mod.photon_batch(heat, heat2, 20000, p)
     first = heat.copy()
     tmc_mod.photon_batch(heat, heat2, 20000, p)       # same photons again: doubles
     assert np.allclose(heat, 2 * first, rtol=1e-6)
-    ref, _, _ = oracle_fx(oracle_mod, 20000, seed=2, **CFG0)
-    h, h2 = oracle_mod.heat_from_tally(oracle_mod.cfg("cfg0"), ref)
+    ref, _, _ = oracle_fx(oracle_mod, 20000, seed=2, **PARAMS_H)
+    h, h2 = oracle_mod.heat_from_tally(oracle_mod.cfg("params_h"), ref)
     assert np.allclose(first, h.astype(np.float32), rtol=1e-6)
     assert np.allclose(heat2, (2 * h2).astype(np.float32), rtol=1e-6)
 
 
 def test_device_entry_point(tmc_mod):
     torch = pytest.importorskip("torch")
-    p = tmc_mod.params(seed=4, **CFG0)
+    p = tmc_mod.params(seed=4, **PARAMS_H)
     d = torch.zeros((101, 4), dtype=torch.int64, device="cuda")
     steps = torch.zeros(1, dtype=torch.int64, device="cuda")
     ws = torch.zeros(tmc_mod.workspace_bytes() // 8, dtype=torch.int64, device="cuda")
     s = torch.cuda.current_stream().cuda_stream
-    p1 = tmc_mod.params(seed=4, photon_id_base=0, **CFG0)
-    p2 = tmc_mod.params(seed=4, photon_id_base=7000, **CFG0)
+    p1 = tmc_mod.params(seed=4, photon_id_base=0, **PARAMS_H)
+    p2 = tmc_mod.params(seed=4, photon_id_base=7000, **PARAMS_H)
     tmc_mod.photon_batch_device(d.data_ptr(), 7000, p1, steps.data_ptr(), ws.data_ptr(), s)
     tmc_mod.photon_batch_device(d.data_ptr(), 13000, p2, steps.data_ptr(), 0, s)
     torch.cuda.synchronize()
     got = d.cpu().numpy().view(np.uint64)
-    ref, ref_steps = gpu_fx(tmc_mod, 20000, seed=4, **CFG0)
+    ref, ref_steps = gpu_fx(tmc_mod, 20000, seed=4, **PARAMS_H)
     assert np.array_equal(got, ref)
     assert int(steps.item()) == ref_steps
     del p
 
 
 @pytest.mark.parametrize("math", ["exact", "fast"])
-def test_vs_fp64_oracle_cfg0(tmc_mod, oracle_mod, math):
+def test_vs_fp64_oracle_params_h(tmc_mod, oracle_mod, math):
     """Gate (a): 1e-4 relative in every shell with >= 1e4 deposits, against
     the FP64 oracle on the same streams (2^20 photons, params.h optics)."""
     n = 1 << 20
-    got, _ = gpu_fx(tmc_mod, n, math=math, **CFG0)
-    p = oracle_mod.cfg("cfg0")
+    got, _ = gpu_fx(tmc_mod, n, math=math, **PARAMS_H)
+    p = oracle_mod.cfg("params_h")
     h, _ = oracle_mod.heat_from_tally(p, got)
     h64, _, dep = oracle_mod.walk_f64(p, n)
     m = dep >= 10000
@@ -182,21 +182,21 @@ def test_vs_fp64_oracle_cfg0(tmc_mod, oracle_mod, math):
     assert rel.max() < 1e-4, rel.max()
 
 
-def test_fast_vs_exact_cfg2(tmc_mod, oracle_mod):
+def test_fast_vs_exact_high_albedo(tmc_mod, oracle_mod):
     """High albedo (7168 steps/photon, 0.001-mfp shells): the FP32 walk itself
     differs from FP64 by shell-boundary flips; the fast arithmetic must stay
     within the same envelope as the exact (= reference) arithmetic."""
     n = 1 << 14
-    ex, _ = gpu_fx(tmc_mod, n, math="exact", **CFG2)
-    fa, _ = gpu_fx(tmc_mod, n, math="fast", **CFG2)
-    p = oracle_mod.cfg("cfg2")
+    ex, _ = gpu_fx(tmc_mod, n, math="exact", **HIGH_ALBEDO)
+    fa, _ = gpu_fx(tmc_mod, n, math="fast", **HIGH_ALBEDO)
+    p = oracle_mod.cfg("high_albedo")
     he, _ = oracle_mod.heat_from_tally(p, ex)
     hf, _ = oracle_mod.heat_from_tally(p, fa)
     h64, _, dep = oracle_mod.walk_f64(p, n)
     m = dep >= 10000
     rel_e = np.abs(he[m] - h64[m]) / h64[m]
     rel_f = np.abs(hf[m] - h64[m]) / h64[m]
-    print(f"cfg2 vs FP64: exact max {rel_e.max():.3g} median {np.median(rel_e):.3g}; "
+    print(f"high_albedo vs FP64: exact max {rel_e.max():.3g} median {np.median(rel_e):.3g}; "
           f"fast max {rel_f.max():.3g} median {np.median(rel_f):.3g}")
     assert rel_f.max() < 3 * rel_e.max() + 1e-4
     assert np.median(rel_f) < 3 * np.median(rel_e) + 1e-5
@@ -207,13 +207,13 @@ def test_native_rng_zscore(tmc_mod, math):
     """Gate (b): GPU (Philox) vs the reference's own libc-rand run (seed 1,
     32768 photons in 32 batches): per-shell |z| <= 4, batch-means sigma."""
     g = np.load(os.path.join(GOLDEN, "ref_native.npz"))
-    ref = g["cfg0_bheat"].astype(np.float64) / int(g["cfg0_batch"])
+    ref = g["params_h_bheat"].astype(np.float64) / int(g["params_h_batch"])
     nb, per = 64, 1 << 14
     means = []
     for b in range(nb):
-        t, _ = gpu_fx(tmc_mod, per, math=math, base=b * per, **CFG0)
+        t, _ = gpu_fx(tmc_mod, per, math=math, base=b * per, **PARAMS_H)
         h = tmc_mod.tally_to_heat(np.ascontiguousarray(t).view(tmc_mod.TALLY_DTYPE).reshape(-1),
-                                  tmc_mod.params(**CFG0))[0]
+                                  tmc_mod.params(**PARAMS_H))[0]
         means.append(h / per)
     means = np.array(means)
     se = np.sqrt(means.var(0, ddof=1) / nb + ref.var(0, ddof=1) / len(ref))

@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 def test_colormap_kernel_matches_oracle(tmc_mod, oracle_mod):
     from tiny_mc_gb300.view import colormap
     g = np.load(os.path.join(GOLDEN, "ref_native.npz"))
-    for heats, w, h in [(g["cfg0_heat"], 800, 800), (g["cfg2_heat"], 640, 480),
+    for heats, w, h in [(g["params_h_heat"], 800, 800), (g["high_albedo_heat"], 640, 480),
                         (np.linspace(0, 3000, 7).astype(np.float32), 1000, 900)]:
         red, rgba = colormap(heats, w, h)
         ored, orgba = oracle_mod.colormap(heats, w, h)
@@ -72,7 +72,7 @@ def test_dropin_driver_output(tmc_mod, tmp_path):
     column agrees with the reference's seed-1 run within statistical noise."""
     import subprocess
     from tiny_mc_gb300 import _build
-    golden = open(os.path.join(GOLDEN, "ref_cfg0_seed1_stdout.txt")).read().splitlines()
+    golden = open(os.path.join(GOLDEN, "ref_params_h_seed1_stdout.txt")).read().splitlines()
     ref = np.array([[float(c) for c in ln.split("\t")] for ln in golden if not ln.startswith("#")])
     for extra_args in ([], ["exact", "fp64", str(tmp_path / "heat.ppm")]):
         out = subprocess.run([_build.DRIVER, "32768", "1"] + extra_args, capture_output=True, text=True,

@@ -14,7 +14,7 @@ from conftest import GOLDEN, ref_tree_available
 
 GOLD_NATIVE = os.path.join(GOLDEN, "ref_native.npz")
 GOLD_INJ = os.path.join(GOLDEN, "ref_injected.npz")
-GOLD_STDOUT = os.path.join(GOLDEN, "ref_cfg0_seed1_stdout.txt")
+GOLD_STDOUT = os.path.join(GOLDEN, "ref_params_h_seed1_stdout.txt")
 
 
 # ------------------------------------------------------------------ Philox
@@ -62,7 +62,7 @@ def test_tmo_logf_accuracy(oracle_mod):
 
 
 # ------------------------------------------- restatement vs reference photon.c
-@pytest.mark.parametrize("name", ["cfg0", "cfg2"])
+@pytest.mark.parametrize("name", ["params_h", "high_albedo"])
 @pytest.mark.parametrize("log_mode", [0, 1])
 def test_restatement_matches_reference_photon_golden(oracle_mod, name, log_mode):
     """Per-photon float arrays of the FP32 restatement are bit-identical to
@@ -77,7 +77,7 @@ def test_restatement_matches_reference_photon_golden(oracle_mod, name, log_mode)
 
 
 @pytest.mark.skipif(not ref_tree_available(), reason="reference tree not present")
-@pytest.mark.parametrize("name,n,base", [("cfg0", 300, 1 << 33), ("cfg2", 8, 977)])
+@pytest.mark.parametrize("name,n,base", [("params_h", 300, 1 << 33), ("high_albedo", 8, 977)])
 def test_restatement_matches_reference_photon_live(oracle_mod, name, n, base):
     oracle_mod.build(ref=True)
     for log_mode in (0, 1):
@@ -89,7 +89,7 @@ def test_restatement_matches_reference_photon_live(oracle_mod, name, n, base):
 def test_native_replay_matches_reference_arrays(oracle_mod):
     """libc-rand replay == the reference's float arrays after srand(1), bitwise."""
     g = np.load(GOLD_NATIVE)
-    for name in ("cfg0", "cfg2"):
+    for name in ("params_h", "high_albedo"):
         n, batch = int(g[f"{name}_n"]), int(g[f"{name}_batch"])
         h, h2, bh, bh2 = oracle_mod.native_run(oracle_mod.cfg(name), n, 1, batch=batch)
         assert np.array_equal(h.view(np.uint32), g[f"{name}_heat"].view(np.uint32))
@@ -109,7 +109,7 @@ def test_fx_tallies_consistent_with_float_walk(oracle_mod):
     """Exact tallies of the restatement against its per-photon float arrays:
     (1-a)*sum_w matches photon.c:30's float sums to float rounding."""
     o = oracle_mod
-    p = o.cfg("cfg0")
+    p = o.cfg("params_h")
     n = 2000
     tally, dep, steps = o.walk_fx(p, n, nthreads=2)
     heat, heat2 = o.heat_from_tally(p, tally)
@@ -122,7 +122,7 @@ def test_fx_tallies_consistent_with_float_walk(oracle_mod):
 
 def test_fx_thread_split_invariance(oracle_mod):
     o = oracle_mod
-    p = o.cfg("cfg0", seed=5)
+    p = o.cfg("params_h", seed=5)
     a = o.walk_fx(p, 3000, id_base=17, nthreads=1)
     b = o.walk_fx(p, 3000, id_base=17, nthreads=7)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2]
@@ -135,11 +135,11 @@ def test_fx_thread_split_invariance(oracle_mod):
     assert s == t
 
 
-def test_fp32_vs_fp64_oracle_cfg0(oracle_mod):
+def test_fp32_vs_fp64_oracle_params_h(oracle_mod):
     """The FP32 walk (photon.c arithmetic) agrees with the FP64 oracle to 1e-4
     in every shell with >= 1e4 deposits at params.h optics."""
     o = oracle_mod
-    p = o.cfg("cfg0")
+    p = o.cfg("params_h")
     n = 1 << 16
     tally, dep, _ = o.walk_fx(p, n, log_mode=o.LOG_NATIVE)
     h32, _ = o.heat_from_tally(p, tally)
@@ -155,15 +155,15 @@ def test_oracle_stat_vs_native_reference(oracle_mod):
     per-shell |z| <= 4 with batch-means sigma on both sides."""
     o = oracle_mod
     g = np.load(GOLD_NATIVE)
-    p = o.cfg("cfg0")
-    ref_b = g["cfg0_bheat"].astype(np.float64)      # 32 batches x 1024 photons
+    p = o.cfg("params_h")
+    ref_b = g["params_h_bheat"].astype(np.float64)      # 32 batches x 1024 photons
     nb, per = 64, 2048
     means = []
     for b in range(nb):
         t, _, _ = o.walk_fx(p, per, id_base=b * per)
         means.append(o.heat_from_tally(p, t)[0] / per)
     means = np.array(means)
-    ref_means = ref_b / int(g["cfg0_batch"])
+    ref_means = ref_b / int(g["params_h_batch"])
     mu_a, se_a = means.mean(0), means.std(0, ddof=1) / np.sqrt(nb)
     mu_b, se_b = ref_means.mean(0), ref_means.std(0, ddof=1) / np.sqrt(len(ref_means))
     z = (mu_a - mu_b) / np.sqrt(se_a ** 2 + se_b ** 2)

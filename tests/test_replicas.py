@@ -42,7 +42,7 @@ def _rank(rank, world, port, n, out_dir):
     from tiny_mc_gb300.replicas import reduce_tallies, shard
     dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
     base, count = shard(n, world, rank, base=12345)
-    t, _, _ = oracle.walk_fx(oracle.cfg("cfg0", seed=3), count, id_base=base, nthreads=2)
+    t, _, _ = oracle.walk_fx(oracle.cfg("params_h", seed=3), count, id_base=base, nthreads=2)
     local = t.reshape(-1).view(TALLY_DTYPE).copy()
     total = reduce_tallies(local)
     np.save(os.path.join(out_dir, f"rank{rank}.npy"), total)
@@ -56,7 +56,7 @@ def test_gloo_two_ranks_match_single_walk(tmp_path, oracle_mod):
         port = s.getsockname()[1]
     n = 6000
     mp.start_processes(_rank, args=(2, port, n, str(tmp_path)), nprocs=2, join=True, start_method="spawn")
-    ref, _, _ = oracle_mod.walk_fx(oracle_mod.cfg("cfg0", seed=3), n, id_base=12345)
+    ref, _, _ = oracle_mod.walk_fx(oracle_mod.cfg("params_h", seed=3), n, id_base=12345)
     for r in range(2):
         got = np.load(tmp_path / f"rank{r}.npy")
         got = np.stack([got["w_lo"], got["w_hi"], got["w2_lo"], got["w2_hi"]], axis=1)

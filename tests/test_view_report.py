@@ -17,8 +17,8 @@ def test_fp64_report_format_matches_float_report(tmc_mod):
     own (float) table to its printed precision."""
     g = np.load(os.path.join(GOLDEN, "ref_native.npz"))
     p = tmc_mod.params()
-    heat = g["cfg0_heat"].astype(np.float64)
-    heat2 = g["cfg0_heat2"].astype(np.float64)
+    heat = g["params_h_heat"].astype(np.float64)
+    heat2 = g["params_h_heat2"].astype(np.float64)
     n = 32768
     t = 4.0 * np.pi * 50.0 ** 3 * n / 1e12
     i = np.arange(100, dtype=np.float64)
@@ -27,7 +27,7 @@ def test_fp64_report_format_matches_float_report(tmc_mod):
     with np.errstate(invalid="ignore"):
         err = np.sqrt(heat2[:100] - heat[:100] ** 2 / n) / t / shell
     text = tmc_mod.format_report_fp64(dens, err, heat[100] / n, p)
-    golden = open(os.path.join(GOLDEN, "ref_cfg0_seed1_stdout.txt")).read()
+    golden = open(os.path.join(GOLDEN, "ref_params_h_seed1_stdout.txt")).read()
     a = parse_table(text)
     b = parse_table("".join(golden.splitlines(keepends=True)[7:]))
     assert a.shape == b.shape == (100, 3)
