@@ -288,7 +288,13 @@ int harvest(tmc_server *s, Wave &w, bool ended)
         }
         const BatchItemDev &it = w.h_items[i];
         const uint64_t id = s->slot_req[it.problem];
-        Req &q = s->active[id];
+        auto f = s->active.find(id);
+        if (f == s->active.end() || f->second.item_photons == 0 ||
+            2 * (it.first / f->second.item_photons) + 1 >= f->second.probe.size()) {
+            set_error_text("server wave: a finished item matches no running request");
+            return TMC_E_STATE;
+        }
+        Req &q = f->second;
         const uint64_t g = it.first / q.item_photons;
         q.probe[2 * g] = e[0];
         q.probe[2 * g + 1] = e[1];
@@ -315,30 +321,26 @@ int harvest(tmc_server *s, Wave &w, bool ended)
     return TMC_OK;
 }
 
-// Fill a wave with pending items, round-robin over the active requests.
+// Fill a wave with pending items: least attained service first (requests
+// with the fewest photon steps issued so far, i.e. new requests' first rounds,
+// go ahead of the later, larger rounds of long-running ones; ties in
+// admission order), at most `quota` items per request.
 int launch_wave(tmc_server *s, Wave &w)
 {
     uint32_t n = 0;
-    size_t pending_reqs = 0;
-    for (uint64_t id : s->order) {
-        const Req &q = s->active[id];
-        if (q.issued < q.next_decision * q.items_per_batch)
-            ++pending_reqs;
-    }
-    if (pending_reqs == 0)
-        return TMC_OK;
-    const uint64_t quota = std::max<uint64_t>(
-        16, std::min<uint64_t>(s->cfg.max_items_per_request, s->wave_cap / pending_reqs));
-    // least attained service first: requests with the fewest photon steps
-    // issued so far (new requests' first rounds) go ahead of the later, larger
-    // rounds of long-running ones; ties in admission order
     std::vector<std::pair<double, uint64_t>> pend;
-    pend.reserve(pending_reqs);
     for (uint64_t id : s->order) {
-        const Req &q = s->active[id];
+        auto f = s->active.find(id);
+        if (f == s->active.end())
+            continue;
+        const Req &q = f->second;
         if (q.issued < q.next_decision * q.items_per_batch)
             pend.push_back({(double)q.issued * q.item_photons * q.est_steps, id});
     }
+    if (pend.empty())
+        return TMC_OK;
+    const uint64_t quota = std::max<uint64_t>(
+        16, std::min<uint64_t>(s->cfg.max_items_per_request, s->wave_cap / pend.size()));
     std::stable_sort(pend.begin(), pend.end(),
                      [](const auto &x, const auto &y) { return x.first < y.first; });
     const uint64_t room = s->cfg.inflight_items
@@ -346,8 +348,7 @@ int launch_wave(tmc_server *s, Wave &w)
                               : ~0ull;
     const uint64_t cap_n = std::min<uint64_t>(s->wave_cap, room);
     for (size_t c = 0; c < pend.size() && n < cap_n; ++c) {
-        const uint64_t id = pend[c].second;
-        Req &q = s->active[id];
+        Req &q = s->active.find(pend[c].second)->second;   // present: collected above
         const uint64_t limit = q.next_decision * q.items_per_batch;
         const uint64_t k = std::min<uint64_t>({limit - q.issued, quota, cap_n - n});
         for (uint64_t j = 0; j < k; ++j) {
