@@ -41,10 +41,11 @@ CPU_PHOTONS_PER_PROC = 1 << 16
 # Issue-slot accounting of walk_plain<256, FastMath> at params.h optics, from
 # ncu --set full of one 2^25-photon launch (profiles/walk_plain_fast_
 # 2p25photons_ncu_full.txt): thread-instructions per photon step and the busy
-# fraction of each pipe.  An SM issues at most 4 warp-instructions per clock.
-WALK_THREAD_INSTR_PER_STEP = 229.6
-WALK_PIPES_NCU = {"issue_slots": 0.796, "alu": 0.543, "fma_heavy": 0.522, "xu_sfu": 0.199,
-                  "shared_wavefronts": 0.504, "dram": 0.0}
+# fraction of each pipe (thread-instructions with the predicate on).  An SM
+# issues at most 4 warp-instructions per clock.
+WALK_THREAD_INSTR_PER_STEP = 223.5
+WALK_PIPES_NCU = {"issue_slots": 0.794, "alu": 0.532, "fma_heavy": 0.529, "xu_sfu": 0.204,
+                  "shared_wavefronts": 0.516, "dram": 0.0}
 # DRAM bytes (read + write) of one walk launch, from an ncu capture of the walk
 # at params.h optics (2^25 photons): only the 101-shell tally flush touches
 # DRAM, so the figure does not grow with the photon count.

@@ -77,9 +77,12 @@ __device__ __forceinline__ float uniform01(uint32_t word)
 
 // 2.0f*rand()/(float)RAND_MAX - 1.0f: 2*fl(r)/2^31 is exact, so one fused
 // multiply-add rounds exactly once where photon.c rounds once (the "- 1").
+// rand31's 0 -> 1 mapping is left out here because it cannot change the
+// result: -1 + 2^-30 rounds to -1.0f (the float spacing next to -1 is 2^-24),
+// the same value r = 0 gives.
 __device__ __forceinline__ float uniform_pm1(uint32_t word)
 {
-    return fmaf(__uint2float_rn(rand31(word)), 0x1p-30f, -1.0f);
+    return fmaf(__uint2float_rn(word >> 1), 0x1p-30f, -1.0f);
 }
 
 // ------------------------------------------------------------ arithmetic
