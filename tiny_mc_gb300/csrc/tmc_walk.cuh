@@ -18,11 +18,12 @@
 //    most retries;
 //  * random words come from a per-thread ring of 16 words in shared memory,
 //    refilled four at a time from Philox; slots 16..21 mirror 0..5 so the
-//    <= 6 words one iteration reads are fixed offsets from one base.  The
-//    refill at the top keeps >= 6 words buffered (an iteration consumes at
-//    most six: step, four for two tries, roulette), runs only when some lane
-//    is short, and then every lane with room refills, so Philox runs with
-//    most lanes active;
+//    <= 6 words one iteration reads are fixed offsets from one base.  An
+//    iteration needs >= 6 buffered words (it consumes at most six: step,
+//    four for two tries, roulette); the refill at the top runs once at least
+//    two walking lanes are short (a short lane waits an iteration rather than
+//    make the whole warp pay for a Philox block it alone uses), and then
+//    every lane with room refills, so Philox runs with most lanes active;
 //  * the two tallies of photon.c:30-31 go into a per-block shared-memory
 //    histogram of 64-bit fixed-point sums (sum of w and of w^2, 2^-40 units),
 //    each kept as two 32-bit words updated with native 32-bit shared atomics
@@ -186,9 +187,17 @@ __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
                 break;
         }
 
-        // -------- keep >= 6 random words buffered (one iteration uses <= 6);
-        // a fresh photon starts empty and needs two passes
-        while (__any_sync(FULL_MASK, alive && (prod - cur) < 6u)) {
+        // -------- refill: an iteration needs >= 6 buffered words (it uses
+        // <= 6).  The warp runs Philox only once at least two walking lanes
+        // are short (or every walking lane is): a refill costs the whole warp
+        // the same issue slots however many lanes take part, so one short
+        // lane waits an iteration instead (the others, using >= 2 words each
+        // per iteration, soon join it).  A fresh photon starts empty and
+        // needs two passes.
+        for (;;) {
+            const unsigned low = __ballot_sync(FULL_MASK, alive && (prod - cur) < 6u);
+            if (low == 0 || (__popc(low) < 2 && low != __ballot_sync(FULL_MASK, alive)))
+                break;
             if (alive && (prod - cur) <= (uint32_t)(RING - 4)) {
                 const uint4 r = philox4x32_10(blk, 0u, pid_lo, pid_hi, keys);
                 ++blk;
@@ -212,7 +221,7 @@ __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
             }
         }
 
-        if (alive) {
+        if (alive && (prod - cur) >= 6u) {   // a short lane waits for the next refill
             // the <= 6 words this iteration may read, from one base
             const uint32_t *rd = my + (cur & (RING - 1)) * BLOCK;
             if (!pending) {
