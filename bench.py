@@ -43,13 +43,13 @@ CPU_PHOTONS_PER_PROC = 1 << 16
 # 2p25photons_ncu_full.txt): thread-instructions per photon step and the busy
 # fraction of each pipe (thread-instructions with the predicate on).  An SM
 # issues at most 4 warp-instructions per clock.
-WALK_THREAD_INSTR_PER_STEP = 223.5
-WALK_PIPES_NCU = {"issue_slots": 0.794, "alu": 0.532, "fma_heavy": 0.529, "xu_sfu": 0.204,
-                  "shared_wavefronts": 0.516, "dram": 0.0}
+WALK_THREAD_INSTR_PER_STEP = 233.2
+WALK_PIPES_NCU = {"issue_slots": 0.811, "alu": 0.537, "fma_heavy": 0.486, "xu_sfu": 0.214,
+                  "shared_wavefronts": 0.511, "dram": 0.0}
 # DRAM bytes (read + write) of one walk launch, from an ncu capture of the walk
 # at params.h optics (2^25 photons): only the 101-shell tally flush touches
 # DRAM, so the figure does not grow with the photon count.
-WALK_DRAM_BYTES_PER_LAUNCH = 19968
+WALK_DRAM_BYTES_PER_LAUNCH = 20736
 
 
 def parse():
