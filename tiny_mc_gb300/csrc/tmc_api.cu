@@ -265,6 +265,7 @@ size_t tmc_workspace_bytes(void) { return WORKSPACE_BYTES; }
 int tmc_photon_batch_fx(tmc_tally *tally, uint64_t n_photons, const tmc_params *p,
                         uint64_t *photon_steps)
 {
+    tmc::NvtxRange nvtx_range("tmc_photon_batch_fx");
     int st = validate(p);
     if (st)
         return st;
@@ -307,6 +308,7 @@ int tmc_photon_batch_fx(tmc_tally *tally, uint64_t n_photons, const tmc_params *
 
 int tmc_photon_batch(float *heat, float *heat2, uint64_t n_photons, const tmc_params *p)
 {
+    tmc::NvtxRange nvtx_range("tmc_photon_batch");
     int st = validate(p);
     if (st)
         return st;
@@ -342,6 +344,7 @@ int tmc_photon_batch(float *heat, float *heat2, uint64_t n_photons, const tmc_pa
 int tmc_photon_batch_device(tmc_tally *d_tally, uint64_t n_photons, const tmc_params *p,
                             uint64_t *d_steps, void *d_workspace, void *stream)
 {
+    tmc::NvtxRange nvtx_range("tmc_photon_batch_device");
     int st = validate(p);
     if (st)
         return st;

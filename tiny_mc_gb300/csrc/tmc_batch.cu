@@ -525,6 +525,7 @@ int tmc_batch_get_config(const tmc_batch *b, tmc_batch_config *cfg)
 
 int tmc_batch_run(tmc_batch *b, void *stream)
 {
+    tmc::NvtxRange nvtx_range("tmc_batch_run");
     if (!b)
         return TMC_E_INVALID;
     std::lock_guard<std::mutex> lk(api_mutex());
@@ -600,6 +601,7 @@ int tmc_expected_steps(float mu_a, float mu_s, double *steps_per_photon)
 
 int tmc_batch_autotune(tmc_batch *b, double scale, double max_steps_per_photon, double *best_ms)
 {
+    tmc::NvtxRange nvtx_range("tmc_batch_autotune");
     if (!b || !(scale > 0.0) || scale > 1.0)
         return TMC_E_INVALID;
     // a reduced copy: photon counts scaled, problems with very long walks left
@@ -675,6 +677,7 @@ int tmc_batch_autotune(tmc_batch *b, double scale, double max_steps_per_photon, 
 
 int tmc_batch_refine(tmc_batch *b, uint32_t max_candidates, double *best_ms)
 {
+    tmc::NvtxRange nvtx_range("tmc_batch_refine");
     if (!b || max_candidates == 0)
         return TMC_E_INVALID;
     if (b->tuned.empty())

@@ -251,6 +251,7 @@ int decide(tmc_server *s, uint64_t id)
     Req &q = f->second;
     if (q.done != q.next_decision * q.items_per_batch)
         return TMC_OK;
+    tmc::NvtxRange nvtx_range("tmc_server decision");
     double m = 0.0;
     const double rse = batch_rse(q.probe, q.items_per_batch, q.next_decision, &m);
     const bool reached = (rse == rse) && rse <= q.r.target_rse;
@@ -327,6 +328,7 @@ int harvest(tmc_server *s, Wave &w, bool ended)
 // admission order), at most `quota` items per request.
 int launch_wave(tmc_server *s, Wave &w)
 {
+    tmc::NvtxRange nvtx_range("tmc_server wave launch");
     uint32_t n = 0;
     std::vector<std::pair<double, uint64_t>> pend;
     for (uint64_t id : s->order) {
@@ -524,6 +526,7 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
 
 int tmc_server_submit(tmc_server *s, const tmc_request *r, uint64_t *id)
 {
+    tmc::NvtxRange nvtx_range("tmc_server_submit");
     if (!s || !r)
         return TMC_E_INVALID;
     tmc_params p;
