@@ -241,6 +241,13 @@ int tmc_batch_autotune(tmc_batch *b, double scale, double max_steps_per_photon, 
  * results do not depend on the configuration.  TMC_E_STATE if autotune has
  * not run.  Not in the reference (it has no batched form). */
 int tmc_batch_refine(tmc_batch *b, uint32_t max_candidates, double *best_ms);
+/* Test hook of the barrier-free kernel's bounded waits (stream = 1): its
+ * waits give up after wait_limit_s seconds of wall time (0 = 120 s), set the
+ * batch's error flag and return, and tmc_batch_read then reports
+ * TMC_E_TIMEOUT.  hold_buffers != 0 stops finished items from freeing their
+ * buffers, so waiting warps run into that limit; the kernel still ends and the
+ * context stays usable.  Not in the reference. */
+int tmc_batch_test_wait(tmc_batch *b, int hold_buffers, double wait_limit_s);
 /* Zeroes the batch's device tallies and walks every problem (asynchronous on
  * stream, a cudaStream_t or NULL). */
 int tmc_batch_run(tmc_batch *b, void *stream);

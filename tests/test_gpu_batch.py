@@ -145,3 +145,32 @@ def test_batch_edge_cases(tmc_mod):
     bad["mu_a"][0] = 0.0
     with pytest.raises(tmc_mod.TmcError):
         tmc_mod.Batch(bad)
+
+
+def test_stream_wait_limit_reports_timeout(tmc_mod):
+    """The barrier-free kernel's only wait (for a block to free an item
+    buffer) is bounded: with the test hook holding every buffer, each block
+    walks two items, its warps wait out a 0.5 s limit, set the error flag and
+    return; the read reports TMC_E_TIMEOUT and the context stays usable."""
+    import time
+    from tiny_mc_gb300.sweep import PROBLEM_DTYPE
+    pr = np.zeros(1, PROBLEM_DTYPE)
+    pr["shells"], pr["microns_per_shell"], pr["mu_a"], pr["mu_s"] = 101, 50.0, 2.0, 20.0
+    pr["n_photons"] = 1 << 22               # ~20 items per block: a third is always needed
+    b = tmc_mod.Batch(pr, seed=1, math="fast")
+    b.set_config(128, 64, False, True)
+    b.run()
+    ref, ref_s = b.read()
+    b.test_wait(True, 0.5)
+    t0 = time.time()
+    b.run()
+    with pytest.raises(tmc_mod.TmcError) as e:
+        b.read()
+    assert e.value.status == -4               # TMC_E_TIMEOUT
+    assert time.time() - t0 < 60
+    b.test_wait(False, 0.0)
+    b.run()
+    t, st = b.read()
+    assert np.array_equal(t, ref) and np.array_equal(st, ref_s)
+    b.close()
+

@@ -105,6 +105,8 @@ def lib() -> ctypes.CDLL:
         L.tmc_batch_autotune.restype = i32
         L.tmc_batch_refine.argtypes = [vp, ctypes.c_uint32, vp]
         L.tmc_batch_refine.restype = i32
+        L.tmc_batch_test_wait.argtypes = [vp, ctypes.c_int, ctypes.c_double]
+        L.tmc_batch_test_wait.restype = i32
         L.tmc_batch_run.argtypes = [vp, vp]
         L.tmc_batch_run.restype = i32
         L.tmc_batch_read.argtypes = [vp, vp, vp]
@@ -261,6 +263,11 @@ class Batch:
         ms = ctypes.c_double(0.0)
         _check(lib().tmc_batch_refine(self.handle, max_candidates, ctypes.byref(ms)), "tmc_batch_refine")
         return ms.value
+
+    def test_wait(self, hold_buffers: bool, wait_limit_s: float = 0.0) -> None:
+        """Test hook of the barrier-free kernel's bounded waits."""
+        _check(lib().tmc_batch_test_wait(self.handle, int(hold_buffers), wait_limit_s),
+               "tmc_batch_test_wait")
 
     def run(self, stream: int = 0) -> None:
         _check(lib().tmc_batch_run(self.handle, stream or None), "tmc_batch_run")

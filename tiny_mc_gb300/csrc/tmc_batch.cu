@@ -195,6 +195,8 @@ struct tmc_batch {
     unsigned long long *d_tally = nullptr;
     unsigned long long *d_steps = nullptr;
     unsigned long long *d_counter = nullptr;
+    unsigned *d_hold = nullptr;          // test hook of walk_stream's waits (tmc_batch_test_wait)
+    unsigned long long wait_limit_ns = 0;
     // graph
     cudaGraphExec_t graph = nullptr;
     cudaStream_t capture_stream = nullptr;
@@ -314,8 +316,10 @@ cudaError_t enqueue(const tmc_batch *b, cudaStream_t s)
     a.error = reinterpret_cast<unsigned *>(b->d_counter + 1);
     a.done_ring = nullptr;
     a.done_tail = nullptr;
+    a.wait_limit_ns = b->wait_limit_ns;
+    a.hold_buffers = b->d_hold;
     if (b->cfg.stream) {
-        // two items open per block: no more blocks than half the items
+        // up to two items open per block, the second claimed when needed
         const int grid = std::max(1, std::min<int>(b->grid, (int)b->n_items));
         return walk_stream_launch(a, b->cfg.block, b->math, grid, s);
     }
@@ -349,6 +353,7 @@ void free_batch(tmc_batch *b)
     cudaFree(b->d_tally);
     cudaFree(b->d_steps);
     cudaFree(b->d_counter);
+    cudaFree(b->d_hold);
     delete b;
 }
 
@@ -738,6 +743,26 @@ int tmc_batch_refine(tmc_batch *b, uint32_t max_candidates, double *best_ms)
     if (best_ms)
         *best_ms = best;
     return st;
+}
+
+int tmc_batch_test_wait(tmc_batch *b, int hold_buffers, double wait_limit_s)
+{
+    if (!b || !(wait_limit_s >= 0.0) || wait_limit_s > 3600.0)
+        return TMC_E_INVALID;
+    std::lock_guard<std::mutex> lk(api_mutex());
+    cudaError_t e = cudaSuccess;
+    if (!b->d_hold)
+        e = cudaMalloc(&b->d_hold, sizeof(unsigned));
+    if (e == cudaSuccess)
+        e = cudaMemset(b->d_hold, hold_buffers ? 1 : 0, sizeof(unsigned));
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "tmc_batch_test_wait");
+    b->wait_limit_ns = (unsigned long long)(wait_limit_s * 1e9);
+    if (b->graph) {   // the captured launch holds the old limit
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return TMC_OK;
 }
 
 int tmc_batch_destroy(tmc_batch *b)

@@ -41,6 +41,11 @@ struct BatchArgs {
     // last word, so the host can take items as they finish.
     unsigned long long *done_ring;
     unsigned *done_tail;
+    // walk_stream's bounded waits: wall-time limit (0 = 120 s), and a test
+    // hook (null in normal runs): while *hold_buffers is nonzero, finished
+    // items' buffers are not freed, so waiting warps run into the limit.
+    unsigned long long wait_limit_ns;
+    const unsigned *hold_buffers;
 };
 
 // Publish a finished item into the completion ring (one thread).  The

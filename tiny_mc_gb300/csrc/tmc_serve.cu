@@ -388,6 +388,8 @@ int launch_wave(tmc_server *s, Wave &w)
         a.error = reinterpret_cast<unsigned *>(w.d_counter + 1);
         a.done_ring = w.d_ring;
         a.done_tail = reinterpret_cast<unsigned *>(w.d_counter + 2);
+        a.wait_limit_ns = 0;
+        a.hold_buffers = nullptr;
         if (s->cfg.stream)
             e = walk_stream_launch(a, (int)s->cfg.block, s->cfg.math,
                                    std::max(1, std::min<int>(s->grid, (int)n)), w.stream);

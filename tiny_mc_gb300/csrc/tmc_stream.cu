@@ -21,8 +21,9 @@
 //    shared record, not in registers, so the kernel keeps the plain walk's
 //    occupancy; photon steps are added to the record when a photon dies;
 //  * waits (a warp with nothing to walk until the block frees a buffer) are
-//    bounded by wall time through %globaltimer: past the limit the warp sets
-//    the error flag and leaves; the host reports TMC_E_TIMEOUT.
+//    bounded by wall time through %globaltimer (120 s unless the launch
+//    says otherwise): past the limit the warp sets the error flag and
+//    leaves; the host reports TMC_E_TIMEOUT.
 // Results are bit-identical to walk_batch and the plain kernel: the same
 // photons, integer sums.
 #include <algorithm>
@@ -36,7 +37,7 @@ namespace tmc {
 namespace {
 
 constexpr uint32_t END_ITEM = 0xffffffffu;
-constexpr unsigned long long WAIT_LIMIT_NS = 120ull * 1000000000ull;
+constexpr unsigned long long DEFAULT_WAIT_LIMIT_NS = 120ull * 1000000000ull;
 constexpr uint32_t BUF_FREE = 0, BUF_CLAIMING = 1, BUF_OPEN = 2;
 
 __device__ __forceinline__ unsigned long long global_ns()
@@ -176,7 +177,11 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
                     hist[s] = 0;
                 __threadfence_block();
                 __syncwarp();
-                if (lane == 0) {
+                unsigned hold = 0;
+                if (lane == 0 && a.hold_buffers)
+                    hold = *(volatile const unsigned *)a.hold_buffers;
+                hold = __shfl_sync(FULL_MASK, hold, 0);
+                if (lane == 0 && !hold) {
                     vopen[rb].state = BUF_FREE;
                     __threadfence_block();
                     vopen[rb].gen = rep + 2;
@@ -271,7 +276,7 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
             const unsigned long long now = global_ns();
             if (wait_start == 0)
                 wait_start = now;
-            else if (now - wait_start > WAIT_LIMIT_NS) {
+            else if (now - wait_start > (a.wait_limit_ns ? a.wait_limit_ns : DEFAULT_WAIT_LIMIT_NS)) {
                 if (lane == 0)
                     atomicExch(a.error, 1u);
                 break;
