@@ -109,3 +109,22 @@ def test_python_mirror_rejects_bad_arrays(tmc_mod):
         tmc_mod.photon_batch(np.zeros(10, np.float32), np.zeros(101, np.float32), 1, p)
     with pytest.raises(ValueError):
         tmc_mod.photon_batch(np.zeros(101, np.float64), np.zeros(101, np.float32), 1, p)
+
+
+def test_batch_and_server_entry_points_reject_null_handles(tmc_mod):
+    """Checked before any CUDA call, so this runs without a GPU."""
+    import ctypes
+    from tiny_mc_gb300 import serve  # noqa: F401  (sets up the server prototypes)
+    serve._setup(tmc_mod.lib())
+    L = tmc_mod.lib()
+    ms = ctypes.c_double(0.0)
+    assert L.tmc_batch_run(None, None) == -1
+    assert L.tmc_batch_autotune(None, 0.5, 0.0, ctypes.byref(ms)) == -1
+    assert L.tmc_batch_refine(None, 4, ctypes.byref(ms)) == -1
+    assert L.tmc_batch_test_wait(None, 1, 0.5) == -1
+    assert L.tmc_batch_destroy(None) == 0
+    assert L.tmc_server_submit(None, None, None) == -1
+    assert L.tmc_server_progress(None, None, None) == -1
+    assert L.tmc_server_run_trace(None, None, None, 0, 0.0, None, None) == -1
+    assert L.tmc_server_destroy(None) == 0
+
