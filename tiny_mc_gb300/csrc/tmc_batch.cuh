@@ -71,7 +71,7 @@ cudaError_t walk_batch_prepare(int block, uint32_t math, uint32_t max_shells, in
 // Launch only (capturable); walk_batch_prepare must have run for this shape.
 cudaError_t walk_batch_launch(const BatchArgs &a, int block, uint32_t math, int grid, cudaStream_t s);
 
-// The barrier-free variant (tmc_stream.cu): two open items per block.
+// The barrier-free variant (tmc_stream.cu): up to two items open per block.
 size_t walk_stream_smem(uint32_t max_shells, int block);
 cudaError_t walk_stream_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid);
 cudaError_t walk_stream_launch(const BatchArgs &a, int block, uint32_t math, int grid, cudaStream_t s);
