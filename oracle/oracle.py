@@ -28,9 +28,13 @@ LOG_TMC = 0
 LOG_NATIVE = 1
 
 CONFIGS = {
-    # name: (shells, microns_per_shell, mu_a, mu_s)
+    # name: (shells, microns_per_shell, mu_a, mu_s); the same optics the
+    # Makefile compiles the reference's photon.c at
     "params_h": (101, 50.0, 2.0, 20.0),
     "high_albedo": (1001, 10.0, 0.1, 100.0),
+    "one_shell": (1, 50.0, 2.0, 20.0),
+    "low_albedo": (101, 50.0, 10.0, 1.0),
+    "fine_shells": (4001, 1.0, 2.0, 20.0),
 }
 
 

@@ -11,13 +11,16 @@ records what those binaries print or compute:
                               srand(1) and N photons (tiny_mc.c:43-49), and
                               per-batch arrays of consecutive photon groups
                               (params_h: 32768 photons = 32 x 1024;
-                              high_albedo: 4096 = 32 x 128), as raw float32
+                              high_albedo: 4096 = 32 x 128; one_shell,
+                              low_albedo: 8192 = 32 x 256; fine_shells: 8192
+                              = 4 x 2048), as raw float32
   ref_injected.npz            per-photon FNV-1a hashes and summed float
                               arrays of the reference's photon() fed by the
                               oracle's Philox streams (seed 1), with the
                               oracle's logarithm (log0) and with libm logf
                               (log1): params_h photons 0..511, high_albedo
-                              photons 0..31
+                              0..31, one_shell 0..511, low_albedo 0..2047,
+                              fine_shells 0..511
 
 Run:  python tests/golden/make_golden.py
 """
@@ -47,7 +50,9 @@ def main() -> None:
 
     # 2. native-RNG arrays and batches
     arrays = {}
-    for name, n, batch in (("params_h", 32768, 1024), ("high_albedo", 4096, 128)):
+    for name, n, batch in (("params_h", 32768, 1024), ("high_albedo", 4096, 128),
+                           ("one_shell", 8192, 256), ("low_albedo", 8192, 256),
+                           ("fine_shells", 8192, 2048)):
         h, h2 = oracle.ref_native_run(name, n, 1)
         bh, bh2 = oracle.ref_native_batches(name, n, 1, batch)
         arrays[f"{name}_n"] = np.array(n)
@@ -60,7 +65,8 @@ def main() -> None:
 
     # 3. the reference's photon() on injected Philox streams
     inj = {}
-    for name, n in (("params_h", 512), ("high_albedo", 32)):
+    for name, n in (("params_h", 512), ("high_albedo", 32), ("one_shell", 512),
+                    ("low_albedo", 2048), ("fine_shells", 512)):
         for log_mode in (oracle.LOG_TMC, oracle.LOG_NATIVE):
             hashes, hs, h2s = oracle.ref_photon_hashes(name, n, seed=1, log_mode=log_mode)
             inj[f"{name}_log{log_mode}_hashes"] = hashes

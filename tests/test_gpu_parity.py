@@ -80,6 +80,19 @@ def test_exact_bit_identical_random_optics(tmc_mod, oracle_mod):
         assert np.array_equal(got, ref), optics
 
 
+@pytest.mark.parametrize("name,n", [("one_shell", 8192), ("low_albedo", 65536), ("fine_shells", 8192)])
+def test_exact_bit_identical_edge_optics(tmc_mod, oracle_mod, name, n):
+    """The optics the oracle is also pinned at against the reference's own
+    photon.c: one shell (every deposit clamped), a roulette every few steps,
+    4001 shells of 1 um (many photons clamped into the last shell)."""
+    shells, mps, mu_a, mu_s = oracle_mod.CONFIGS[name]
+    optics = dict(shells=shells, microns_per_shell=mps, mu_a=mu_a, mu_s=mu_s)
+    got, steps = gpu_fx(tmc_mod, n, seed=11, base=1 << 36, **optics)
+    ref, _, ref_steps = oracle_fx(oracle_mod, n, seed=11, base=1 << 36, **optics)
+    assert steps == ref_steps
+    assert np.array_equal(got, ref)
+
+
 @pytest.mark.parametrize("shells,mps,n,nt", [(20000, 0.5, 4096, 0), (1 << 24, 0.001, 64, 1)])
 def test_exact_bit_identical_wide_tallies(tmc_mod, oracle_mod, shells, mps, n, nt):
     """Shell counts whose histogram does not fit in shared memory: deposits go

@@ -62,7 +62,10 @@ def test_tmo_logf_accuracy(oracle_mod):
 
 
 # ------------------------------------------- restatement vs reference photon.c
-@pytest.mark.parametrize("name", ["params_h", "high_albedo"])
+EDGE_OPTICS = ["one_shell", "low_albedo", "fine_shells"]
+
+
+@pytest.mark.parametrize("name", ["params_h", "high_albedo"] + EDGE_OPTICS)
 @pytest.mark.parametrize("log_mode", [0, 1])
 def test_restatement_matches_reference_photon_golden(oracle_mod, name, log_mode):
     """Per-photon float arrays of the FP32 restatement are bit-identical to
@@ -77,7 +80,9 @@ def test_restatement_matches_reference_photon_golden(oracle_mod, name, log_mode)
 
 
 @pytest.mark.skipif(not ref_tree_available(), reason="reference tree not present")
-@pytest.mark.parametrize("name,n,base", [("params_h", 300, 1 << 33), ("high_albedo", 8, 977)])
+@pytest.mark.parametrize("name,n,base", [("params_h", 300, 1 << 33), ("high_albedo", 8, 977),
+                                         ("one_shell", 300, 5), ("low_albedo", 2000, 1 << 40),
+                                         ("fine_shells", 300, 12345)])
 def test_restatement_matches_reference_photon_live(oracle_mod, name, n, base):
     oracle_mod.build(ref=True)
     for log_mode in (0, 1):
@@ -89,7 +94,7 @@ def test_restatement_matches_reference_photon_live(oracle_mod, name, n, base):
 def test_native_replay_matches_reference_arrays(oracle_mod):
     """libc-rand replay == the reference's float arrays after srand(1), bitwise."""
     g = np.load(GOLD_NATIVE)
-    for name in ("params_h", "high_albedo"):
+    for name in ["params_h", "high_albedo"] + EDGE_OPTICS:
         n, batch = int(g[f"{name}_n"]), int(g[f"{name}_batch"])
         h, h2, bh, bh2 = oracle_mod.native_run(oracle_mod.cfg(name), n, 1, batch=batch)
         assert np.array_equal(h.view(np.uint32), g[f"{name}_heat"].view(np.uint32))
