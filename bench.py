@@ -38,14 +38,14 @@ METRIC = "photons/s on 1 GB300 (plain vs batched/served) at stated error; p50/p9
 UNIT = "photons/s"
 SFU_OPS_PER_STEP = 4          # log, sqrt (radius), divide + sqrt (direction)
 CPU_PHOTONS_PER_PROC = 1 << 16
-# Issue-slot accounting of walk_plain<256, FastMath> at params.h optics, from
+# Issue-slot accounting of walk_plain<512, FastMath> at params.h optics, from
 # ncu --set full of one 2^25-photon launch (profiles/walk_plain_fast_
 # 2p25photons_ncu_full.txt): thread-instructions per photon step and the busy
 # fraction of each pipe (thread-instructions with the predicate on).  An SM
 # issues at most 4 warp-instructions per clock.
-WALK_THREAD_INSTR_PER_STEP = 233.2
-WALK_PIPES_NCU = {"issue_slots": 0.811, "alu": 0.537, "fma_heavy": 0.486, "xu_sfu": 0.214,
-                  "shared_wavefronts": 0.511, "dram": 0.0}
+WALK_THREAD_INSTR_PER_STEP = 232.2
+WALK_PIPES_NCU = {"issue_slots": 0.815, "alu": 0.544, "fma_heavy": 0.489, "xu_sfu": 0.216,
+                  "shared_wavefronts": 0.515, "dram": 0.0}
 # DRAM bytes (read + write) of one walk launch, from an ncu capture of the walk
 # at params.h optics (2^25 photons): only the 101-shell tally flush touches
 # DRAM, so the figure does not grow with the photon count.

@@ -340,7 +340,7 @@ int tmc_server_destroy(tmc_server *s);
 
 /*
  * Launch shape of the plain walk: threads per block (128, 256 or 512; 0 =
- * default), resident blocks per SM (0 = occupancy limit) and a cap on the
+ * default, 512), resident blocks per SM (0 = occupancy limit) and a cap on the
  * grid (0 = none).  Results do not depend on it (integer tallies,
  * photon-keyed streams); only speed does.
  */
