@@ -338,6 +338,19 @@ int tmc_server_run_trace(tmc_server *s, const tmc_request *reqs, const double *a
                          double time_limit_s, tmc_request_result *results, uint32_t *completed);
 int tmc_server_destroy(tmc_server *s);
 
+/* The server's plan for a request, computed on the host without a device:
+ * photons per RSE batch, work items per batch and the expected photon steps
+ * per photon it was sized from.  Not in the reference. */
+int tmc_server_plan(const tmc_server_config *cfg, const tmc_request *r, uint32_t *batch_photons,
+                    uint32_t *items_per_batch, double *steps_per_photon);
+/* The server's stop statistic, on the host: batch-means relative standard
+ * error of n_batches batches, batch j's value being the exact 128-bit sum of
+ * its items' probes probes[2 i] (low 64 bits) and probes[2 i + 1] (high),
+ * i = j * items_per_batch .. + items_per_batch - 1, converted to weight units
+ * (2^-40) once; NaN when the mean is not positive.  Not in the reference. */
+int tmc_batch_means_rse(const uint64_t *probes, uint32_t items_per_batch, uint64_t n_batches,
+                        double *rse, double *mean);
+
 /*
  * Launch shape of the plain walk: threads per block (128, 256 or 512; 0 =
  * default, 512), resident blocks per SM (0 = occupancy limit) and a cap on the

@@ -438,6 +438,33 @@ int progress_locked(tmc_server *s)
     return TMC_OK;
 }
 
+bool config_valid(const tmc_server_config &c)
+{
+    return c.slots > 0 && c.slots <= (1u << 20) && c.max_shells > 0 && c.max_shells <= (1u << 16) &&
+           c.min_batches >= 2 && c.max_items_per_request > 0 && c.steps_per_batch > 0.0 &&
+           c.steps_per_item >= 0.0 && c.waves <= (uint32_t)WAVES &&
+           (c.math == TMC_MATH_EXACT || c.math == TMC_MATH_FAST) &&
+           (c.block == 128 || c.block == 256 || c.block == 512);
+}
+
+// The request's knobs as tmc_params checks them, plus the server's own limits.
+int request_valid(const tmc_server_config &c, const tmc_request &r)
+{
+    tmc_params p;
+    tmc_params_default(&p);
+    p.shells = r.shells;
+    p.microns_per_shell = r.microns_per_shell;
+    p.mu_a = r.mu_a;
+    p.mu_s = r.mu_s;
+    int st = validate(&p);
+    if (st)
+        return st;
+    if (r.shells > c.max_shells || !(r.target_rse > 0.0) || r.max_photons == 0 ||
+        r.max_photons > (1ull << 40) || r.photon_id_base > ~0ull - r.max_photons)
+        return TMC_E_INVALID;
+    return TMC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -463,11 +490,7 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
     if (!out || !cfg)
         return TMC_E_INVALID;
     *out = nullptr;
-    if (cfg->slots == 0 || cfg->slots > (1u << 20) || cfg->max_shells == 0 ||
-        cfg->max_shells > (1u << 16) || cfg->min_batches < 2 || cfg->max_items_per_request == 0 ||
-        !(cfg->steps_per_batch > 0.0) || !(cfg->steps_per_item >= 0.0) || cfg->waves > (uint32_t)WAVES ||
-        (cfg->math != TMC_MATH_EXACT && cfg->math != TMC_MATH_FAST) ||
-        (cfg->block != 128 && cfg->block != 256 && cfg->block != 512))
+    if (!config_valid(*cfg))
         return TMC_E_INVALID;
     std::lock_guard<std::mutex> lk(api_mutex());
     int st = TMC_OK;
@@ -531,18 +554,9 @@ int tmc_server_submit(tmc_server *s, const tmc_request *r, uint64_t *id)
     tmc::NvtxRange nvtx_range("tmc_server_submit");
     if (!s || !r)
         return TMC_E_INVALID;
-    tmc_params p;
-    tmc_params_default(&p);
-    p.shells = r->shells;
-    p.microns_per_shell = r->microns_per_shell;
-    p.mu_a = r->mu_a;
-    p.mu_s = r->mu_s;
-    int st = validate(&p);
+    int st = request_valid(s->cfg, *r);
     if (st)
         return st;
-    if (r->shells > s->cfg.max_shells || !(r->target_rse > 0.0) || r->max_photons == 0 ||
-        r->max_photons > (1ull << 40) || r->photon_id_base > ~0ull - r->max_photons)
-        return TMC_E_INVALID;
     std::lock_guard<std::mutex> lk(api_mutex());
     if (s->free_slots.empty())
         return TMC_E_BUSY;
@@ -732,6 +746,39 @@ int tmc_server_run_trace(tmc_server *s, const tmc_request *reqs, const double *a
     }
     if (completed)
         *completed = done;
+    return TMC_OK;
+}
+
+int tmc_server_plan(const tmc_server_config *cfg, const tmc_request *r, uint32_t *batch,
+                    uint32_t *items_per_batch_out, double *steps_per_photon)
+{
+    if (!cfg || !r || !config_valid(*cfg))
+        return TMC_E_INVALID;
+    const int st = request_valid(*cfg, *r);
+    if (st)
+        return st;
+    const Derived d = derive(r->mu_a, r->mu_s, r->microns_per_shell, r->shells);
+    const double est = expected_steps_host(d.albedo);
+    const uint32_t b = batch_photons(*cfg, est);
+    if (batch)
+        *batch = b;
+    if (items_per_batch_out)
+        *items_per_batch_out = items_per_batch(*cfg, b, est);
+    if (steps_per_photon)
+        *steps_per_photon = est;
+    return TMC_OK;
+}
+
+int tmc_batch_means_rse(const uint64_t *probes, uint32_t items_per_batch_in, uint64_t n_batches,
+                        double *rse, double *mean)
+{
+    if (!probes || items_per_batch_in == 0 || n_batches == 0 || !rse)
+        return TMC_E_INVALID;
+    std::vector<unsigned long long> v(probes, probes + 2 * (size_t)items_per_batch_in * n_batches);
+    double m = 0.0;
+    *rse = batch_rse(v, items_per_batch_in, n_batches, &m);
+    if (mean)
+        *mean = m;
     return TMC_OK;
 }
 

@@ -73,6 +73,10 @@ def _setup(L):
     L.tmc_server_run_trace.restype = i32
     L.tmc_server_destroy.argtypes = [vp]
     L.tmc_server_destroy.restype = i32
+    L.tmc_server_plan.argtypes = [SC, vp, vp, vp, vp]
+    L.tmc_server_plan.restype = i32
+    L.tmc_batch_means_rse.argtypes = [vp, ctypes.c_uint32, u64, vp, vp]
+    L.tmc_batch_means_rse.restype = i32
     L._serve_ready = True
 
 
@@ -84,6 +88,31 @@ def default_config(**kw) -> ServerConfig:
     for k, v in kw.items():
         setattr(c, k, v)
     return c
+
+
+def plan(request, config: ServerConfig | None = None, **kw):
+    """``tmc_server_plan`` (host only): (photons per RSE batch, work items per
+    batch, expected photon steps per photon) the server would use."""
+    L = lib()
+    _setup(L)
+    c = config if config is not None else default_config(**kw)
+    r = np.ascontiguousarray(np.asarray(request, REQUEST_DTYPE).reshape(1))
+    b, k, e = ctypes.c_uint32(0), ctypes.c_uint32(0), ctypes.c_double(0.0)
+    _check(L.tmc_server_plan(ctypes.byref(c), r.ctypes.data, ctypes.byref(b), ctypes.byref(k),
+                             ctypes.byref(e)), "tmc_server_plan")
+    return b.value, k.value, e.value
+
+
+def batch_means_rse(probes: np.ndarray, items_per_batch: int, n_batches: int):
+    """``tmc_batch_means_rse`` (host only): probes uint64 [items][2] (low, high
+    64 bits of each item's 128-bit sum); returns (rse, mean)."""
+    L = lib()
+    _setup(L)
+    p = np.ascontiguousarray(probes, np.uint64)
+    rse, mean = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    _check(L.tmc_batch_means_rse(p.ctypes.data, items_per_batch, n_batches, ctypes.byref(rse),
+                                 ctypes.byref(mean)), "tmc_batch_means_rse")
+    return rse.value, mean.value
 
 
 class Server:
