@@ -260,6 +260,13 @@ int tmc_batch_info(const tmc_batch *b, uint32_t *n_items, double *est_photon_ste
  * recursion (albedo^k, roulette at 0.001 with survival 0.1, photon.c:32,45-49)
  * evaluated on the host.  The batch planner splits work with it. */
 int tmc_expected_steps(float mu_a, float mu_s, double *steps_per_photon);
+/* The batch planner on the host, for a given resident grid: the work items
+ * (problem, first photon, photon count) a batch would walk, heaviest first,
+ * as items_out[3 i .. 3 i + 2].  *n_items receives the count; with capacity
+ * 0 only the count is computed, a smaller nonzero capacity returns
+ * TMC_E_OVERFLOW.  No device needed.  Not in the reference. */
+int tmc_batch_plan_items(const tmc_problem *problems, uint32_t n_problems, int grid, int block,
+                         int items_per_block, uint64_t *items_out, uint64_t capacity, uint64_t *n_items);
 /* Device address of the batch's tallies (valid until destroy). */
 const void *tmc_batch_device_tallies(const tmc_batch *b);
 int tmc_batch_destroy(tmc_batch *b);

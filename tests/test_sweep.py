@@ -46,3 +46,67 @@ def test_expected_steps_known_values(tmc_mod):
     # 24 per survival), 7168 at the high-albedo optics
     assert abs(tmc_mod.expected_steps(2.0, 20.0) - 75.667) < 0.01
     assert abs(tmc_mod.expected_steps(0.1, 100.0) - 7168.0) < 1.0
+
+
+# ----------------------------------------------------- the batch planner (host)
+def _check_partition(pr, items):
+    """Every problem's photon range [0, n) is covered exactly once."""
+    for i in range(len(pr)):
+        mine = items[items[:, 0] == i]
+        mine = mine[np.argsort(mine[:, 1])]
+        n = int(pr["n_photons"][i])
+        if n == 0:
+            assert len(mine) == 0
+            continue
+        assert int(mine[0, 1]) == 0
+        assert np.all(mine[1:, 1] == mine[:-1, 1] + mine[:-1, 2])
+        assert int(mine[-1, 1] + mine[-1, 2]) == n
+        assert np.all(mine[:, 2] > 0) and np.all(mine[:, 2] < 1 << 30)
+
+
+@pytest.mark.parametrize("grid,block,ipb", [(1520, 128, 8), (456, 512, 16), (7, 256, 1), (3000, 128, 64)])
+def test_plan_items_partition_and_order(tmc_mod, grid, block, ipb):
+    from tiny_mc_gb300.sweep import make_sweep
+    pr = make_sweep(300, seed=4, photon_scale=1.0 / 64, min_photons=16)
+    pr["n_photons"][::37] = 0                       # empty problems get no items
+    items = tmc_mod.plan_items(pr, grid, block, ipb)
+    _check_partition(pr, items)
+    est = np.array([tmc_mod.expected_steps(float(a), float(b)) for a, b in zip(pr["mu_a"], pr["mu_s"])])
+    work = est[items[:, 0].astype(int)] * items[:, 2]
+    assert np.all(work[:-1] >= work[1:])            # heaviest first
+    for i in range(len(pr)):                        # no item below one photon per lane, unless
+        n = int(pr["n_photons"][i])                 # the problem is that small
+        k = int(np.sum(items[:, 0] == i))
+        assert k <= max(1, -(-n // block))
+
+
+def test_plan_items_one_photon_per_lane_rule(tmc_mod):
+    """A problem whose photons are so long that two in a row would reach the
+    launch's expected steps per lane is split down to one photon per lane;
+    otherwise items keep two photons per lane."""
+    from tiny_mc_gb300.sweep import PROBLEM_DTYPE
+    pr = np.zeros(2, PROBLEM_DTYPE)
+    pr["shells"], pr["microns_per_shell"] = 101, 50.0
+    pr["mu_a"], pr["mu_s"] = [0.01, 2.0], [1000.0, 20.0]      # ~7e5 and ~76 steps per photon
+    grid, block = 100, 128
+    pr["n_photons"] = [4096, 1000]
+    items = tmc_mod.plan_items(pr, grid, block, 8)
+    heavy = items[items[:, 0] == 0]
+    assert len(heavy) == 4096 // block and np.all(heavy[:, 2] == block)
+    pr["n_photons"] = [4096, 1 << 30]               # light work dominates: lanes have room
+    items = tmc_mod.plan_items(pr, grid, block, 8)
+    heavy = items[items[:, 0] == 0]
+    assert len(heavy) == 4096 // (2 * block) and np.all(heavy[:, 2] == 2 * block)
+    _check_partition(pr, items)
+
+
+def test_plan_items_rejects_bad_input(tmc_mod):
+    from tiny_mc_gb300.sweep import PROBLEM_DTYPE
+    pr = np.zeros(1, PROBLEM_DTYPE)
+    pr["shells"], pr["microns_per_shell"], pr["mu_a"], pr["mu_s"], pr["n_photons"] = 101, 50.0, 0.0, 20.0, 10
+    with pytest.raises(tmc_mod.TmcError):
+        tmc_mod.plan_items(pr, 10, 128, 8)          # mu_a = 0
+    pr["mu_a"] = 2.0
+    with pytest.raises(tmc_mod.TmcError):
+        tmc_mod.plan_items(pr, 0, 128, 8)           # no grid
+

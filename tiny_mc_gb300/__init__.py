@@ -119,6 +119,9 @@ def lib() -> ctypes.CDLL:
         L.tmc_batch_device_tallies.restype = vp
         L.tmc_batch_destroy.argtypes = [vp]
         L.tmc_batch_destroy.restype = i32
+        L.tmc_batch_plan_items.argtypes = [vp, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           vp, u64, vp]
+        L.tmc_batch_plan_items.restype = i32
         L.tmc_expected_steps.argtypes = [ctypes.c_float, ctypes.c_float, vp]
         L.tmc_expected_steps.restype = i32
         L.tmc_photon_batch_static.argtypes = [vp, vp, u64, P, vp]
@@ -221,6 +224,21 @@ def expected_steps(mu_a: float, mu_s: float) -> float:
     out = ctypes.c_double(0.0)
     _check(lib().tmc_expected_steps(mu_a, mu_s, ctypes.byref(out)), "tmc_expected_steps")
     return out.value
+
+
+def plan_items(problems, grid: int, block: int, items_per_block: int) -> np.ndarray:
+    """``tmc_batch_plan_items`` (host only): the work items a batch would walk
+    on `grid` resident blocks, heaviest first, as uint64 [n][3] (problem,
+    first photon, photon count)."""
+    from .sweep import PROBLEM_DTYPE
+    pr = np.ascontiguousarray(problems, PROBLEM_DTYPE)
+    n = ctypes.c_uint64(0)
+    _check(lib().tmc_batch_plan_items(pr.ctypes.data, len(pr), grid, block, items_per_block, None, 0,
+                                      ctypes.byref(n)), "tmc_batch_plan_items")
+    out = np.zeros((max(1, n.value), 3), np.uint64)
+    _check(lib().tmc_batch_plan_items(pr.ctypes.data, len(pr), grid, block, items_per_block,
+                                      out.ctypes.data, n.value, ctypes.byref(n)), "tmc_batch_plan_items")
+    return out[:n.value]
 
 
 class Batch:

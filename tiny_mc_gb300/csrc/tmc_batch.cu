@@ -220,32 +220,32 @@ cudaError_t grid_for(const tmc_batch *b, int *grid)
 }
 
 // Split problems into items of about equal estimated photon steps.
-int plan(tmc_batch *b)
+// Split problems into work items (photon-id ranges) of about equal
+// estimated photon steps for `grid` resident blocks of `block` threads with
+// `items_per_block` items each, heaviest first.  Host only.
+std::vector<BatchItemDev> plan_items(const std::vector<tmc_problem> &problems,
+                                     const std::vector<double> &est_steps, int grid, int block,
+                                     int items_per_block)
 {
-    int grid = 0;
-    cudaError_t e = grid_for(b, &grid);   // also sets the kernel's shared-memory limit
-    if (e != cudaSuccess)
-        return set_cuda_error(e, "batch kernel config");
-    b->grid = grid;
     double total = 0.0;
-    for (size_t i = 0; i < b->problems.size(); ++i)
-        total += b->est_steps[i] * (double)b->problems[i].n_photons;
-    const double target = std::max(1.0, total / ((double)grid * std::max(1, b->cfg.items_per_block)));
+    for (size_t i = 0; i < problems.size(); ++i)
+        total += est_steps[i] * (double)problems[i].n_photons;
+    const double target = std::max(1.0, total / ((double)grid * std::max(1, items_per_block)));
     // Smallest item: two photons per thread of the block (a lane whose first
     // photon dies early takes a second one), or one photon per thread for a
     // problem whose photons are so long (high albedo: up to ~1e6 steps, each
     // walked serially by one lane) that two of them in a row would reach the
     // launch's expected steps per lane: spread one per lane, such photons
     // start in the first items and do not set the end of the launch.
-    const double lane_steps = total / ((double)grid * b->cfg.block);
+    const double lane_steps = total / ((double)grid * block);
     std::vector<std::pair<double, BatchItemDev>> items;
-    for (size_t i = 0; i < b->problems.size(); ++i) {
-        const unsigned long long n = b->problems[i].n_photons;
+    for (size_t i = 0; i < problems.size(); ++i) {
+        const unsigned long long n = problems[i].n_photons;
         if (n == 0)
             continue;
         const unsigned long long min_item =
-            (unsigned long long)b->cfg.block * (2.0 * b->est_steps[i] <= lane_steps ? 2 : 1);
-        const double work = b->est_steps[i] * (double)n;
+            (unsigned long long)block * (2.0 * est_steps[i] <= lane_steps ? 2 : 1);
+        const double work = est_steps[i] * (double)n;
         unsigned long long k = (unsigned long long)std::ceil(work / target);
         k = std::max(1ull, std::min(k, (n + min_item - 1) / min_item));
         k = std::max(k, (n + 0x3fffffffull) / 0x40000000ull);   // counts stay below 2^30
@@ -258,7 +258,7 @@ int plan(tmc_batch *b)
             it.count = (uint32_t)c;
             it.first = at;
             at += c;
-            items.push_back({b->est_steps[i] * (double)c, it});
+            items.push_back({est_steps[i] * (double)c, it});
         }
     }
     std::stable_sort(items.begin(), items.end(),
@@ -266,6 +266,18 @@ int plan(tmc_batch *b)
     std::vector<BatchItemDev> h(items.size());
     for (size_t i = 0; i < items.size(); ++i)
         h[i] = items[i].second;
+    return h;
+}
+
+int plan(tmc_batch *b)
+{
+    int grid = 0;
+    cudaError_t e = grid_for(b, &grid);   // also sets the kernel's shared-memory limit
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "batch kernel config");
+    b->grid = grid;
+    const std::vector<BatchItemDev> h =
+        plan_items(b->problems, b->est_steps, grid, b->cfg.block, b->cfg.items_per_block);
     if (h.size() > b->items_cap) {
         if (b->d_items)
             cudaFree(b->d_items);
@@ -588,6 +600,38 @@ int tmc_batch_info(const tmc_batch *b, uint32_t *n_items, double *est_photon_ste
 }
 
 const void *tmc_batch_device_tallies(const tmc_batch *b) { return b ? b->d_tally : nullptr; }
+
+int tmc_batch_plan_items(const tmc_problem *problems, uint32_t n_problems, int grid, int block,
+                         int items_per_block, uint64_t *items_out, uint64_t capacity, uint64_t *n_items)
+{
+    if ((n_problems && !problems) || !n_items || grid < 1 || block < 32 || items_per_block < 1 ||
+        (capacity && !items_out))
+        return TMC_E_INVALID;
+    std::vector<tmc_problem> pr(problems, problems + n_problems);
+    std::vector<double> est(n_problems);
+    for (uint32_t i = 0; i < n_problems; ++i) {
+        tmc_params p;
+        tmc_params_default(&p);
+        p.shells = pr[i].shells;
+        p.microns_per_shell = pr[i].microns_per_shell;
+        p.mu_a = pr[i].mu_a;
+        p.mu_s = pr[i].mu_s;
+        const int st = validate(&p);
+        if (st)
+            return st;
+        est[i] = expected_steps(derive(p.mu_a, p.mu_s, p.microns_per_shell, p.shells).albedo);
+    }
+    const std::vector<BatchItemDev> h = plan_items(pr, est, grid, block, items_per_block);
+    *n_items = h.size();
+    if (h.size() > capacity)
+        return capacity ? TMC_E_OVERFLOW : TMC_OK;
+    for (size_t i = 0; i < h.size(); ++i) {
+        items_out[3 * i] = h[i].problem;
+        items_out[3 * i + 1] = h[i].first;
+        items_out[3 * i + 2] = h[i].count;
+    }
+    return TMC_OK;
+}
 
 int tmc_expected_steps(float mu_a, float mu_s, double *steps_per_photon)
 {
