@@ -375,7 +375,9 @@ int tmc_debug_rand(uint64_t seed, uint64_t photon, uint32_t n, int32_t *out);
  * denominator of the walk's SFU roofline.  No reference counterpart. */
 int tmc_probe_sfu_rate(double *mufu_ops_per_s);
 
-/* Text of a status code, and the last CUDA error message seen. */
+/* Text of a status code, and the detail of the calling thread's last
+ * failed call (kept per thread, like errno; valid until that thread's next
+ * failure). */
 const char *tmc_strerror(int status);
 const char *tmc_last_error(void);
 

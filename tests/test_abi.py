@@ -128,3 +128,24 @@ def test_batch_and_server_entry_points_reject_null_handles(tmc_mod):
     assert L.tmc_server_run_trace(None, None, None, 0, 0.0, None, None) == -1
     assert L.tmc_server_destroy(None) == 0
 
+
+def test_error_text_is_specific_and_per_thread(tmc_mod):
+    import ctypes
+    import threading
+    L = tmc_mod.lib()
+    h = np.zeros(101, np.float32)
+    p = tmc_mod.params(shells=(1 << 24) + 1)
+    assert L.tmc_photon_batch(h.ctypes.data, h.ctypes.data, 10, ctypes.byref(p)) == -1
+    mine = L.tmc_last_error()
+    assert b"shells" in mine
+
+    def other():
+        q = tmc_mod.params(mu_a=0.0)
+        assert L.tmc_photon_batch(h.ctypes.data, h.ctypes.data, 10, ctypes.byref(q)) == -1
+        assert b"mu_a" in L.tmc_last_error()
+
+    t = threading.Thread(target=other)
+    t.start()
+    t.join()
+    assert L.tmc_last_error() == mine          # another thread's failure left ours alone
+

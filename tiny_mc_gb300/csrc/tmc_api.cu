@@ -12,7 +12,7 @@ namespace tmc {
 
 namespace {
 std::mutex g_mutex;
-std::string g_error;
+thread_local std::string g_error;   // per thread, like errno
 DeviceCtx g_ctx[64];
 int g_plain_block = 0;
 int g_plain_blocks_per_sm = 0;
@@ -38,26 +38,30 @@ int set_cuda_error(cudaError_t e, const char *where)
 
 int validate(const tmc_params *p)
 {
+    auto invalid = [](const char *why) {
+        set_error_text(std::string("invalid parameters: ") + why);
+        return TMC_E_INVALID;
+    };
     if (!p)
-        return TMC_E_INVALID;
+        return invalid("null tmc_params");
     if (p->shells == 0 || p->shells > (1u << 24))
-        return TMC_E_INVALID;
+        return invalid("shells must be 1 .. 2^24");
     // MU_A "!!non-zero!!" (params.h:14): with mu_a = 0 the weight never
     // decays and a photon never dies.
     if (!(p->mu_a > 0.0f) || !std::isfinite(p->mu_a))
-        return TMC_E_INVALID;
+        return invalid("mu_a must be finite and > 0");
     if (!(p->mu_s >= 0.0f) || !std::isfinite(p->mu_s))
-        return TMC_E_INVALID;
+        return invalid("mu_s must be finite and >= 0");
     if (!(p->microns_per_shell > 0.0f) || !std::isfinite(p->microns_per_shell))
-        return TMC_E_INVALID;
+        return invalid("microns_per_shell must be finite and > 0");
     if (p->math != TMC_MATH_EXACT && p->math != TMC_MATH_FAST)
-        return TMC_E_INVALID;
+        return invalid("math must be TMC_MATH_EXACT or TMC_MATH_FAST");
     if (p->reserved != 0)
-        return TMC_E_INVALID;
+        return invalid("reserved must be 0");
     // If mu_a is so small against mu_s that the float albedo rounds to 1, the
     // weight never decays (photon.c:32) and no photon would ever die.
     if (!(p->mu_s / (p->mu_s + p->mu_a) < 1.0f))
-        return TMC_E_INVALID;
+        return invalid("mu_a too small against mu_s: the float albedo rounds to 1");
     return TMC_OK;
 }
 
@@ -220,11 +224,12 @@ static int run_into_ctx_tally(DeviceCtx &c, uint64_t n, const tmc_params *p, con
     return TMC_OK;
 }
 
-static int check_sizes(uint64_t n, const tmc_params *p, const DeviceCtx &c)
+static int check_sizes(uint64_t n, const tmc_params *p)
 {
-    (void)c;
-    if (n > (1ull << 62) || p->photon_id_base > ~0ull - n)
+    if (n > (1ull << 62) || p->photon_id_base > ~0ull - n) {
+        set_error_text("photon count or photon_id_base + count overflows 64-bit photon ids");
         return TMC_E_OVERFLOW;
+    }
     return TMC_OK;
 }
 
@@ -275,7 +280,7 @@ int tmc_photon_batch_fx(tmc_tally *tally, uint64_t n_photons, const tmc_params *
     DeviceCtx *c = current_ctx(&st);
     if (!c)
         return st;
-    if ((st = check_sizes(n_photons, p, *c)))
+    if ((st = check_sizes(n_photons, p)))
         return st;
     const Derived d = derive(p->mu_a, p->mu_s, p->microns_per_shell, p->shells);
     unsigned long long *d_steps = reinterpret_cast<unsigned long long *>(c->workspace) + 1;
@@ -318,7 +323,7 @@ int tmc_photon_batch(float *heat, float *heat2, uint64_t n_photons, const tmc_pa
     DeviceCtx *c = current_ctx(&st);
     if (!c)
         return st;
-    if ((st = check_sizes(n_photons, p, *c)))
+    if ((st = check_sizes(n_photons, p)))
         return st;
     const Derived d = derive(p->mu_a, p->mu_s, p->microns_per_shell, p->shells);
     if ((st = run_into_ctx_tally(*c, n_photons, p, d, nullptr)))
@@ -354,7 +359,7 @@ int tmc_photon_batch_device(tmc_tally *d_tally, uint64_t n_photons, const tmc_pa
     DeviceCtx *c = current_ctx(&st);
     if (!c)
         return st;
-    if ((st = check_sizes(n_photons, p, *c)))
+    if ((st = check_sizes(n_photons, p)))
         return st;
     if (n_photons == 0)
         return TMC_OK;
