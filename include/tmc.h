@@ -16,7 +16,9 @@
  * Thread safety: like photon() (global rand, unsynchronised +=), the library
  * is meant to be driven by one host thread at a time per process; calls are
  * serialised by an internal lock so concurrent calls are safe but not
- * concurrent.
+ * concurrent.  Device scratch the library owns is ordered on the GPU as well:
+ * an asynchronous call that uses it (tmc_photon_batch_device with no
+ * workspace) finishes on the GPU before any later call touches it.
  */
 #ifndef TMC_H
 #define TMC_H
@@ -108,8 +110,13 @@ size_t tmc_workspace_bytes(void);
  * Device-resident form: d_tally is DEVICE memory [p->shells] and is added to
  * (+=).  d_steps (device, may be NULL) += photon steps.  d_workspace is
  * device scratch of tmc_workspace_bytes() bytes, or NULL to use a buffer the
- * library allocates once per device.  stream is a cudaStream_t (NULL =
- * legacy default stream).  Asynchronous: returns after the launch.
+ * library allocates once per device.  That shared buffer is also the one the
+ * host-array calls use: every use of it, on any stream, first waits on the
+ * GPU for the previous use to end, so calls with NULL on different streams
+ * run one after another (bring a workspace per stream to overlap them).
+ * Under stream capture that ordering is not recorded: pass a workspace when
+ * capturing.  stream is a cudaStream_t (NULL = legacy default stream).
+ * Asynchronous: returns after the launch.
  */
 int tmc_photon_batch_device(tmc_tally *d_tally, uint64_t n_photons, const tmc_params *p,
                             uint64_t *d_steps, void *d_workspace, void *stream);
@@ -120,10 +127,14 @@ int tmc_photon_batch_device(tmc_tally *d_tally, uint64_t n_photons, const tmc_pa
  * memory.  For callers that cannot let a library call cudaMalloc — device
  * memory owned by another allocator, or a loop that forbids allocation after
  * start-up.  Its device scratch (claim counter, tallies, FP64 results) is a
- * fixed array of TMC_STATIC_SCRATCH_BYTES inside the library, held by every
- * GPU that loads the library until the process exits.  shells above
- * TMC_STATIC_MAX_SHELLS return TMC_E_INVALID.  The first call on a device
- * looks up that array's device address; make it before any stream capture.
+ * fixed array of TMC_STATIC_SCRATCH_BYTES inside the library's module, held
+ * by a GPU from the moment the module is loaded on it until the process
+ * exits.  shells above TMC_STATIC_MAX_SHELLS return TMC_E_INVALID.  The first
+ * call on a device loads the module there (under CUDA's default lazy loading
+ * this is a driver allocation) and looks up the array's device address: make
+ * that call during start-up and before any stream capture; n_photons = 0 does
+ * only this set-up.  The address is kept for the device's primary context:
+ * not supported after cudaDeviceReset or under another current context.
  * All calls share the array (each clears what it uses first); calls are
  * serialised and synchronous, and two of them running at once on the GPU
  * would race.  stream: a cudaStream_t or NULL.

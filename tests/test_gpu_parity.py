@@ -180,11 +180,35 @@ def test_device_entry_point(tmc_mod):
     del p
 
 
-@pytest.mark.parametrize("math", ["exact", "fast"])
-def test_vs_fp64_oracle_params_h(tmc_mod, oracle_mod, math):
+def test_device_form_shared_workspace_is_ordered(tmc_mod, oracle_mod):
+    """tmc_photon_batch_device with no workspace uses the library's own photon
+    claim counter, the one the host-array calls use too.  A device-form walk
+    still running on a side stream (one block, so it lasts) must not have that
+    counter reset under it by a host-array call made right after it on the
+    library's stream: both tallies must equal the oracle's bit for bit."""
+    torch = pytest.importorskip("torch")
+    n_dev, n_host = 1 << 16, 4096
+    d = torch.zeros((101, 4), dtype=torch.int64, device="cuda")
+    side = torch.cuda.Stream()
+    tmc_mod.set_plain_launch(512, 1, 1)
+    p_dev = tmc_mod.params(seed=21, photon_id_base=0, **PARAMS_H)
+    with torch.cuda.stream(side):
+        tmc_mod.photon_batch_device(d.data_ptr(), n_dev, p_dev, 0, 0, side.cuda_stream)
+    host, host_steps = gpu_fx(tmc_mod, n_host, seed=21, base=n_dev, **PARAMS_H)
+    side.synchronize()
+    dev = d.cpu().numpy().view(np.uint64)
+    ref_dev, _, _ = oracle_fx(oracle_mod, n_dev, seed=21, base=0, **PARAMS_H)
+    ref_host, _, ref_host_steps = oracle_fx(oracle_mod, n_host, seed=21, base=n_dev, **PARAMS_H)
+    assert np.array_equal(dev, ref_dev)
+    assert np.array_equal(host, ref_host) and host_steps == ref_host_steps
+
+
+@pytest.mark.parametrize("math,n", [("exact", 1 << 20), ("fast", 1 << 20), ("exact", 1 << 24),
+                                    ("fast", 1 << 24)])
+def test_vs_fp64_oracle_params_h(tmc_mod, oracle_mod, math, n):
     """Gate (a): 1e-4 relative in every shell with >= 1e4 deposits, against
-    the FP64 oracle on the same streams (2^20 photons, params.h optics)."""
-    n = 1 << 20
+    the FP64 oracle on the same streams (params.h optics; 2^24 photons is the
+    largest count the FP64 oracle walks in seconds on the host's cores)."""
     got, _ = gpu_fx(tmc_mod, n, math=math, **PARAMS_H)
     p = oracle_mod.cfg("params_h")
     h, _ = oracle_mod.heat_from_tally(p, got)
@@ -192,6 +216,7 @@ def test_vs_fp64_oracle_params_h(tmc_mod, oracle_mod, math):
     m = dep >= 10000
     assert m.sum() >= 100
     rel = np.abs(h[m] - h64[m]) / h64[m]
+    print(f"{math} 2^{n.bit_length() - 1} photons vs FP64: max rel {rel.max():.3g} over {m.sum()} shells")
     assert rel.max() < 1e-4, rel.max()
 
 
@@ -232,3 +257,35 @@ def test_native_rng_zscore(tmc_mod, math):
     se = np.sqrt(means.var(0, ddof=1) / nb + ref.var(0, ddof=1) / len(ref))
     z = (means.mean(0) - ref.mean(0)) / se
     assert np.all(np.abs(z[:-1]) < 4.0), np.abs(z).max()
+
+
+@pytest.mark.parametrize("math", ["exact", "fast"])
+def test_native_rng_zscore_high_albedo(tmc_mod, math):
+    """Gate (b) at high-albedo optics (1001 shells of 10 um, ~7168 steps per
+    photon): GPU (Philox, 64 batches of 2^12 photons) against the reference's
+    own libc-rand run (seed 1, 4096 photons in 32 batches of 128), batch-means
+    sigma.  The reference's 128-photon batches make each of the 1000 shells'
+    sigma a 31-degree-of-freedom estimate, so |z| <= 4 is applied to the heat
+    of 32-shell groups (one test per group, 32 groups), and per shell at 5.4,
+    the threshold whose chance of being crossed once among 1000 shells under
+    the null equals that of 4 sigma for a single shell (two-sided 6.3e-5)."""
+    g = np.load(os.path.join(GOLDEN, "ref_native.npz"))
+    ref = g["high_albedo_bheat"].astype(np.float64) / int(g["high_albedo_batch"])
+    nb, per = 64, 1 << 12
+    means = []
+    for b in range(nb):
+        t, _ = gpu_fx(tmc_mod, per, math=math, base=b * per, **HIGH_ALBEDO)
+        h = tmc_mod.tally_to_heat(np.ascontiguousarray(t).view(tmc_mod.TALLY_DTYPE).reshape(-1),
+                                  tmc_mod.params(**HIGH_ALBEDO))[0]
+        means.append(h / per)
+    means = np.array(means)
+    se = np.sqrt(means.var(0, ddof=1) / nb + ref.var(0, ddof=1) / len(ref))
+    z = (means.mean(0) - ref.mean(0)) / se
+    gi = np.arange(1000) // 32
+    grp = lambda a: np.stack([np.bincount(gi, weights=row[:1000]) for row in a])  # noqa: E731
+    gm, gr = grp(means), grp(ref)
+    zg = (gm.mean(0) - gr.mean(0)) / np.sqrt(gm.var(0, ddof=1) / nb + gr.var(0, ddof=1) / len(gr))
+    print(f"high_albedo {math}: max |z| per 32-shell group {np.abs(zg).max():.2f}, "
+          f"per shell {np.abs(z[:-1]).max():.2f}, last shell {z[-1]:.2f}")
+    assert np.all(np.abs(zg) < 4.0)
+    assert np.all(np.abs(z) < 5.4)

@@ -110,10 +110,35 @@ DeviceCtx *current_ctx(int *status)
             *status = set_cuda_error(e, "cudaStreamCreate");
             return nullptr;
         }
+        e = cudaEventCreateWithFlags(&c.ws_done, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            *status = set_cuda_error(e, "cudaEventCreate");
+            return nullptr;
+        }
         c.device = dev;
     }
     *status = TMC_OK;
     return &c;
+}
+
+static bool capturing(cudaStream_t stream)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
+cudaError_t ws_acquire(DeviceCtx &c, cudaStream_t stream)
+{
+    if (capturing(stream))
+        return cudaSuccess;
+    return cudaStreamWaitEvent(stream, c.ws_done, 0);
+}
+
+cudaError_t ws_release(DeviceCtx &c, cudaStream_t stream)
+{
+    if (capturing(stream))
+        return cudaSuccess;
+    return cudaEventRecord(c.ws_done, stream);
 }
 
 static int ensure_buffers(DeviceCtx &c, uint32_t shells)
@@ -203,6 +228,8 @@ static int run_into_ctx_tally(DeviceCtx &c, uint64_t n, const tmc_params *p, con
         return st;
     cudaError_t e = cudaMemsetAsync(c.tally, 0, sizeof(tmc_tally) * p->shells, c.stream);
     if (e == cudaSuccess)
+        e = ws_acquire(c, c.stream);
+    if (e == cudaSuccess)
         e = cudaMemsetAsync(c.workspace, 0, WORKSPACE_BYTES, c.stream);
     if (e != cudaSuccess)
         return set_cuda_error(e, "cudaMemsetAsync");
@@ -222,6 +249,13 @@ static int run_into_ctx_tally(DeviceCtx &c, uint64_t n, const tmc_params *p, con
     if (e != cudaSuccess)
         return set_cuda_error(e, "walk_plain launch");
     return TMC_OK;
+}
+
+// After the host-array calls' reads of the step counter.
+static int release_ctx_workspace(DeviceCtx &c)
+{
+    const cudaError_t e = ws_release(c, c.stream);
+    return e == cudaSuccess ? TMC_OK : set_cuda_error(e, "cudaEventRecord(workspace)");
 }
 
 static int check_sizes(uint64_t n, const tmc_params *p)
@@ -292,6 +326,8 @@ int tmc_photon_batch_fx(tmc_tally *tally, uint64_t n_photons, const tmc_params *
                                     cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(&steps, d_steps, sizeof steps, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && (st = release_ctx_workspace(*c)))
+        return st;
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess)
@@ -327,6 +363,8 @@ int tmc_photon_batch(float *heat, float *heat2, uint64_t n_photons, const tmc_pa
         return st;
     const Derived d = derive(p->mu_a, p->mu_s, p->microns_per_shell, p->shells);
     if ((st = run_into_ctx_tally(*c, n_photons, p, d, nullptr)))
+        return st;
+    if ((st = release_ctx_workspace(*c)))
         return st;
     const uint32_t S = p->shells;
     cudaError_t e = launch_tally_to_heat(c->tally, S, (double)d.c, c->heat_out, c->heat_out + S,
@@ -365,7 +403,9 @@ int tmc_photon_batch_device(tmc_tally *d_tally, uint64_t n_photons, const tmc_pa
         return TMC_OK;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     void *ws = d_workspace ? d_workspace : c->workspace;
-    cudaError_t e = cudaMemsetAsync(ws, 0, sizeof(unsigned long long), s);
+    cudaError_t e = d_workspace ? cudaSuccess : ws_acquire(*c, s);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(ws, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess)
         return set_cuda_error(e, "cudaMemsetAsync(workspace)");
     PlainLaunch L{};
@@ -379,6 +419,8 @@ int tmc_photon_batch_device(tmc_tally *d_tally, uint64_t n_photons, const tmc_pa
     L.blocks_per_sm = g_plain_blocks_per_sm;
     L.max_blocks = g_plain_max_blocks;
     e = launch_plain(L, *c, s);
+    if (e == cudaSuccess && !d_workspace)
+        e = ws_release(*c, s);
     if (e != cudaSuccess)
         return set_cuda_error(e, "walk_plain launch");
     return TMC_OK;

@@ -47,6 +47,7 @@ struct DeviceCtx {
     double *heat_out = nullptr;         // 2 * out_cap doubles
     size_t out_cap = 0;
     cudaStream_t stream = nullptr;
+    cudaEvent_t ws_done = nullptr;      // recorded after the last use of workspace
 };
 
 // Returns the context of the current device (creating it), or nullptr with
@@ -57,6 +58,15 @@ int set_cuda_error(cudaError_t e, const char *where);
 void set_error_text(const std::string &s);
 
 constexpr size_t WORKSPACE_BYTES = 256;
+
+// The context's workspace (photon claim counter, step counter) is shared by
+// the host-array calls and by device-form calls that bring no workspace of
+// their own, on whatever stream each uses.  ws_acquire makes `stream` wait on
+// the GPU until the previous use has finished; ws_release marks the end of
+// this use.  A stream under capture is left alone (the ordering would not be
+// part of the graph; callers that capture pass their own workspace).
+cudaError_t ws_acquire(DeviceCtx &c, cudaStream_t stream);
+cudaError_t ws_release(DeviceCtx &c, cudaStream_t stream);
 
 // Plain walk launch (tmc_plain.cu).  d_work points at a zeroed 64-bit photon
 // claim counter.
@@ -73,9 +83,6 @@ struct PlainLaunch {
 };
 cudaError_t launch_plain(const PlainLaunch &L, const DeviceCtx &ctx, cudaStream_t stream);
 size_t plain_smem_bytes(uint32_t shells, int block);
-// Largest shell count whose shared-memory histogram fits at the default
-// block; launch_plain walks larger counts with global-memory deposits.
-int plain_max_shells(const DeviceCtx &ctx);
 
 // FP64 finalisation on the device (tmc_api.cu).
 cudaError_t launch_tally_to_heat(const tmc_tally *d_tally, uint32_t shells, double c,
