@@ -67,11 +67,6 @@ static uint32_t histogram_max_shells(const DeviceCtx &ctx, int block)
     return cap > ring ? (uint32_t)((cap - ring) / 16) : 0u;
 }
 
-int plain_max_shells(const DeviceCtx &ctx)
-{
-    return (int)histogram_max_shells(ctx, 256);
-}
-
 template <int BLOCK, class M, bool WIDE>
 static cudaError_t launch_t(const PlainLaunch &L, const DeviceCtx &ctx, cudaStream_t stream)
 {

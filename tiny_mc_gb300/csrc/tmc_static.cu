@@ -8,18 +8,25 @@
 // caching pool that must see every byte), a real-time loop that forbids
 // allocation after start-up, or a plugin host that hands out memory itself.
 // This entry point keeps that scratch in a fixed file-scope __device__ array
-// instead.  The array exists on every GPU that loads the library, from load
-// until the process exits, whether or not this entry point is used.
+// instead.  The array belongs to the library's module: a GPU holds it from the
+// moment the module is loaded on it until the process exits.  Under lazy
+// module loading (the CUDA default) that moment is the first call of this
+// entry point on that device, so the first call itself makes the driver load
+// the module (and the walk and finalisation kernels it launches): make it
+// during start-up, before any stream capture; a call with n_photons = 0 does
+// exactly that set-up and walks nothing.
 //
 // Host code cannot use the array's name as a device address (in host code it
 // names a host-side stand-in), so the first call on each device, with that
-// device current, looks the address up with cudaGetSymbolAddress and keeps it.
-// Because of that look-up, the first call on a device should come before any
-// stream capture.  Every call shares the one array and it keeps the last
-// call's contents: each call clears the claim counter and the tallies it uses
-// before its walk.  Calls are serialised by the library's lock and wait for
-// their own work, so calls through this entry point never overlap; work that
-// ran two of them at once on the GPU would race on the shared array.
+// device current, looks the address up with cudaGetSymbolAddress and keeps
+// it.  The kept address belongs to the device's primary context: after
+// cudaDeviceReset, or when the caller makes another context current on the
+// device, it is stale, and that use is not supported.  Every call shares the
+// one array and it keeps the last call's contents: each call clears the claim
+// counter and the tallies it uses before its walk.  Calls are serialised by
+// the library's lock and wait for their own work, so calls through this entry
+// point never overlap; work that ran two of them at once on the GPU would race
+// on the shared array.
 #include <cstring>
 
 #include "tmc_device.cuh"
@@ -53,22 +60,29 @@ extern "C" int tmc_photon_batch_static(float *heat, float *heat2, uint64_t n_pho
     int st = validate(p);
     if (st)
         return st;
-    if (!heat || !heat2)
+    if (!heat || !heat2) {
+        set_error_text("tmc_photon_batch_static: heat or heat2 is NULL");
         return TMC_E_INVALID;
+    }
     if (p->shells > TMC_STATIC_MAX_SHELLS) {
         set_error_text("tmc_photon_batch_static: shells > TMC_STATIC_MAX_SHELLS (4096)");
         return TMC_E_INVALID;
     }
-    if (n_photons > (1ull << 62) || p->photon_id_base > ~0ull - n_photons)
+    if (n_photons > (1ull << 62) || p->photon_id_base > ~0ull - n_photons) {
+        set_error_text("tmc_photon_batch_static: photon count or photon_id_base + count overflows "
+                       "64-bit photon ids");
         return TMC_E_OVERFLOW;
+    }
     std::lock_guard<std::mutex> lk(api_mutex());
 
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
         return set_cuda_error(e, "cudaGetDevice");
-    if (dev < 0 || dev >= 64)
+    if (dev < 0 || dev >= 64) {
+        set_error_text("tmc_photon_batch_static: device ordinal outside 0..63");
         return TMC_E_NODEVICE;
+    }
     if (!g_static_addr[dev]) {
         void *ptr = nullptr;
         e = cudaGetSymbolAddress(&ptr, g_static_scratch);
@@ -86,10 +100,6 @@ extern "C" int tmc_photon_batch_static(float *heat, float *heat2, uint64_t n_pho
     c.device = dev;
     c.sms = sms;
     c.smem_optin = (size_t)optin;
-    if ((int64_t)p->shells > plain_max_shells(c)) {
-        set_error_text("tmc_photon_batch_static: shells exceed the shared-memory histogram");
-        return TMC_E_INVALID;
-    }
 
     unsigned char *base = static_cast<unsigned char *>(g_static_addr[dev]);
     unsigned long long *work = reinterpret_cast<unsigned long long *>(base);
@@ -103,18 +113,18 @@ extern "C" int tmc_photon_batch_static(float *heat, float *heat2, uint64_t n_pho
     if (e != cudaSuccess)
         return set_cuda_error(e, "cudaMemsetAsync(static scratch)");
     const Derived d = derive(p->mu_a, p->mu_s, p->microns_per_shell, S);
-    if (n_photons > 0) {
-        PlainLaunch L{};
-        L.p = p;
-        L.d = d;
-        L.n_photons = n_photons;
-        L.d_tally = tally;
-        L.d_work = work;
-        L.d_steps = nullptr;
-        e = launch_plain(L, c, s);
-        if (e != cudaSuccess)
-            return set_cuda_error(e, "walk_plain launch (static)");
-    }
+    // launched even for zero photons (one block that walks nothing), so that a
+    // zero-photon first call also loads the walk kernel
+    PlainLaunch L{};
+    L.p = p;
+    L.d = d;
+    L.n_photons = n_photons;
+    L.d_tally = tally;
+    L.d_work = work;
+    L.d_steps = nullptr;
+    e = launch_plain(L, c, s);
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "walk_plain launch (static)");
     e = launch_tally_to_heat(tally, S, (double)d.c, heat_out, heat_out + S, s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(g_static_host, heat_out, sizeof(double) * 2 * S, cudaMemcpyDeviceToHost, s);
