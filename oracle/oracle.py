@@ -22,7 +22,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_TREE = os.environ.get("TMC_REFERENCE_TREE", "/root/reference")
+# the reference's source tree: $TMC_REFERENCE_TREE, else a directory named
+# "reference" beside this repository's root
+REFERENCE_TREE = os.environ.get("TMC_REFERENCE_TREE") or os.path.normpath(
+    os.path.join(HERE, os.pardir, os.pardir, "reference"))
 
 LOG_TMC = 0
 LOG_NATIVE = 1

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Needs the reference tree (computacionparalela/tiny_mc) — by default
-/root/reference, or $TMC_REFERENCE_TREE — and gcc.  It builds oracle/_ref/
+Needs the reference tree (computacionparalela/tiny_mc) — $TMC_REFERENCE_TREE,
+else a directory named "reference" beside this repository — and gcc.  It builds oracle/_ref/
 (the reference's own sources compiled unchanged, see oracle/Makefile) and
 records what those binaries print or compute:
 

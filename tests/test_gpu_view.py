@@ -69,11 +69,21 @@ def test_report_fp64_matches_host_formula(tmc_mod):
 def test_dropin_driver_output(tmc_mod, tmp_path):
     """The drop-in tiny_mc prints the reference's layout: 7 header lines, the
     two timing lines, the two column titles, 100 rows and "# extra"; its heat
-    column agrees with the reference's seed-1 run within statistical noise."""
+    column agrees with the reference's seed-1 run (libc rand, 32768 photons)
+    within |z| <= 4 in every shell.  Sigma is batch means: the reference's
+    32 batches of 1024 photons give the variance of a 32768-photon total, and
+    the drop-in's run (same photon count, other streams) has the same, so the
+    difference's variance is twice it."""
     import subprocess
     from tiny_mc_gb300 import _build
     golden = open(os.path.join(GOLDEN, "ref_params_h_seed1_stdout.txt")).read().splitlines()
     ref = np.array([[float(c) for c in ln.split("\t")] for ln in golden if not ln.startswith("#")])
+    g = np.load(os.path.join(GOLDEN, "ref_native.npz"))
+    bheat = g["params_h_bheat"].astype(np.float64)
+    var_total = len(bheat) * bheat.var(0, ddof=1)
+    i = np.arange(100, dtype=np.float64)
+    vol = 4.0 * np.pi * 50.0 ** 3 * 32768 / 1e12 * (i * i + i + 1.0 / 3.0)
+    sigma_density = np.sqrt(2.0 * var_total[:100]) / vol
     for extra_args in ([], ["exact", "fp64", str(tmp_path / "heat.ppm")]):
         out = subprocess.run([_build.DRIVER, "32768", "1"] + extra_args, capture_output=True, text=True,
                              check=True).stdout.splitlines()
@@ -82,8 +92,8 @@ def test_dropin_driver_output(tmc_mod, tmp_path):
         assert out[7].startswith("# ") and out[7].endswith("seconds")
         rows = np.array([[float(c) for c in ln.split("\t")] for ln in out[11:111]])
         assert np.array_equal(rows[:, 0], ref[:, 0])
-        rel = np.abs(rows[:60, 1] - ref[:60, 1]) / ref[:60, 1]
-        assert rel.max() < 0.08, rel.max()
+        z = (rows[:, 1] - ref[:, 1]) / sigma_density
+        assert np.abs(z).max() < 4.0, (np.abs(z).max(), int(np.abs(z).argmax()))
         assert out[-1].startswith("# extra\t")
     ppm = (tmp_path / "heat.ppm").read_bytes()
     assert ppm.startswith(b"P6\n800 800\n255\n") and len(ppm) == len(b"P6\n800 800\n255\n") + 800 * 800 * 3
