@@ -119,6 +119,9 @@ def parse():
                     help="server launches in flight (1..64; -1: library default)")
     ap.add_argument("--serve-stream", type=int, choices=[-1, 0, 1], default=-1,
                     help="server kernel: 0 per-item barriers, 1 barrier-free, -1 library default")
+    ap.add_argument("--serve-persistent", type=int, choices=[-1, 0, 1], default=-1,
+                    help="server: 1 one persistent launch fed from a work queue, 0 waves of launches, "
+                         "-1 library default")
     ap.add_argument("--serve-calib", type=int, default=256)
     ap.add_argument("--serve-window", type=float, default=5.0)
     ap.add_argument("--serve-duration", type=float, default=30.0)
@@ -740,6 +743,8 @@ def serve_leg(args, device_id):
         kw["waves"] = args.serve_waves
     if args.serve_inflight_items >= 0:
         kw["inflight_items"] = args.serve_inflight_items
+    if args.serve_persistent >= 0:
+        kw["persistent"] = args.serve_persistent
     math = 1 if args.math == "fast" else 0
     clocks = ClockSampler(device_id)
     clocks.start()
@@ -764,7 +769,8 @@ def serve_leg(args, device_id):
     lat_o = res_o["latency_s"][got]
     s.close()
     s = Server(slots=args.serve_slots, math=math, **kw)
-    kernel = "barrier-free" if s.cfg.stream else "per-item barriers"
+    kernel = ("barrier-free, one persistent launch fed from a work queue" if s.cfg.persistent else
+              "barrier-free, waves of launches" if s.cfg.stream else "per-item barriers, waves of launches")
     rate = 0.7 * saturated / mean_steps
     n3 = max(50, min(int(rate * args.serve_duration), n_total - C))
     sel3 = slice(C, C + n3)

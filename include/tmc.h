@@ -330,7 +330,14 @@ typedef struct tmc_server_config {
     uint32_t waves;                 /* launches in flight at once, 1..64 (0 = 16) */
     uint32_t inflight_items;        /* work items launched and not yet finished: no new
                                        items above it, so new requests do not queue behind
-                                       long-running ones (0 = unbounded) */
+                                       long-running ones (0 = unbounded; with persistent,
+                                       0 = twice the resident blocks) */
+    uint32_t persistent;            /* 1: instead of launches per wave, a long-running
+                                       launch of the barrier-free kernel takes items from a
+                                       work queue in mapped host memory that the server
+                                       keeps filling (least attained service first); its
+                                       blocks wait for work while requests are active and
+                                       end once none are (waves and stream do not apply) */
 } tmc_server_config;
 
 typedef struct tmc_server tmc_server;

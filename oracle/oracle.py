@@ -74,6 +74,8 @@ def lib() -> ctypes.CDLL:
         L.tmo_philox4x32_10.argtypes = [vp, vp, vp]
         L.tmo_logf.argtypes = [ctypes.c_float]
         L.tmo_logf.restype = ctypes.c_float
+        L.tmo_logf_max_ulp.argtypes = [ctypes.c_float, ctypes.c_float, u32, vp]
+        L.tmo_logf_max_ulp.restype = ctypes.c_double
         L.tmo_stream_dump.argtypes = [u64, u64, u32, vp]
         L.tmo_walk_fx.argtypes = [P, u64, u64, i32, vp, vp, vp, i32]
         L.tmo_walk_fx.restype = i32
@@ -117,6 +119,14 @@ def stream(seed: int, photon: int, n: int) -> np.ndarray:
 
 def logf(x: float) -> float:
     return lib().tmo_logf(x)
+
+
+def logf_max_ulp(lo: float, hi: float, stride: int = 1):
+    """(largest ulp error of tmo_logf against double log over every stride-th
+    float of [lo, hi], share correctly rounded)."""
+    share = ctypes.c_double(0.0)
+    worst = lib().tmo_logf_max_ulp(lo, hi, stride, ctypes.byref(share))
+    return worst, share.value
 
 
 def walk_fx(p: OParams, n: int, id_base: int = 0, log_mode: int = LOG_TMC, nthreads: int = 0):

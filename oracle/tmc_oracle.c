@@ -95,12 +95,14 @@ static inline uint32_t u_of(float f)
 
 /*
  * Natural logarithm for positive normal floats (the walk only asks for
- * x in [2^-31, 1]).  x = 2^k * m with m in [sqrt(1/2), sqrt(2)); then
- * log(m) = 2 atanh(s), s = (m-1)/(m+1), summed as the odd Taylor series of
- * atanh through s^9 (|s| <= 0.1716, truncation below 2^-28 relative), and
+ * x in [2^-31, 1]): the library's own division-free sequence, the one the
+ * GPU's exact arithmetic evaluates.  x = 2^k * m with m in [sqrt(1/2),
+ * sqrt(2)), f = m - 1 (exact), log(m) = f + f^2 R(f) with R the degree-8
+ * polynomial oracle/logfit.py derives (Chebyshev interpolant of log1p(f)/f,
+ * coefficients rounded to float) evaluated by Horner with fmaf, and
  * log(x) = k*ln2_hi + (k*ln2_lo + log(m)) with ln2 split so k*ln2_hi is exact.
- * Every operation is one IEEE-rounded float op; the GPU kernel evaluates the
- * same sequence with __fmul_rn/__fadd_rn/__fdiv_rn and gets the same bits.
+ * Every operation is one IEEE-rounded op (fmaf rounds once); the GPU kernel
+ * evaluates the same sequence with __fmul_rn/__fmaf_rn and gets the same bits.
  */
 float tmo_logf(float x)
 {
@@ -108,22 +110,46 @@ float tmo_logf(float x)
     int32_t k = (int32_t)((ix + 0x004afb0du) >> 23) - 127;
     float m = f_of(ix - ((uint32_t)k << 23));
     float f = m - 1.0f;
-    float s = f / (2.0f + f);
-    float z = s * s;
-    float pz = 0.222222222f;    /* 2/9 */
-    pz = pz * z;
-    pz = pz + 0.285714286f;     /* 2/7 */
-    pz = pz * z;
-    pz = pz + 0.4f;             /* 2/5 */
-    pz = pz * z;
-    pz = pz + 0.666666667f;     /* 2/3 */
-    float sz = s * z;
-    float tail = sz * pz;
-    float lm = (s + s) + tail;
+    float f2 = f * f;
+    float r = -0x1.31335ap-4f;
+    r = fmaf(r, f, 0x1.064786p-3f);
+    r = fmaf(r, f, -0x1.0fb036p-3f);
+    r = fmaf(r, f, 0x1.22cf10p-3f);
+    r = fmaf(r, f, -0x1.5423b0p-3f);
+    r = fmaf(r, f, 0x1.999e86p-3f);
+    r = fmaf(r, f, -0x1.000424p-2f);
+    r = fmaf(r, f, 0x1.55555ep-2f);
+    r = fmaf(r, f, -0x1.fffff8p-2f);
+    float lm = fmaf(f2, r, f);
     float kf = (float)k;
-    float hi = kf * 0.693145751953125f;
-    float lo = kf * 1.42860682e-6f;
-    return hi + (lo + lm);
+    return fmaf(kf, 0.693145751953125f, fmaf(kf, 1.42860682e-6f, lm));
+}
+
+/* Largest error of tmo_logf in ulps against the C library's double log over
+ * the floats from lo to hi (bit patterns, every `stride`-th), and the share of
+ * them that tmo_logf rounds correctly. */
+double tmo_logf_max_ulp(float lo, float hi, uint32_t stride, double *correct_share)
+{
+    double worst = 0.0;
+    uint64_t n = 0, exact = 0;
+    if (stride == 0)
+        stride = 1;
+    for (uint64_t u = u_of(lo); u <= u_of(hi); u += stride) {
+        const float x = f_of((uint32_t)u);
+        const float y = tmo_logf(x);
+        const double t = log((double)x);
+        const float ft = (float)fabs(t);
+        const double spacing = (double)nextafterf(ft, INFINITY) - (double)ft;
+        const double e = t == 0.0 ? fabs((double)y) : fabs((double)y - t) / spacing;
+        if ((float)t == y)
+            ++exact;
+        if (e > worst)
+            worst = e;
+        ++n;
+    }
+    if (correct_share)
+        *correct_share = n ? (double)exact / (double)n : 0.0;
+    return worst;
 }
 
 /* ------------------------------------------------------ derived constants */

@@ -54,6 +54,9 @@ void tmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 
 /* The logarithm shared bit-for-bit with the GPU kernel's exact mode. */
 float tmo_logf(float x);
+/* Its largest error in ulps (against the C library's double log) over every
+ * stride-th float of [lo, hi], and the share of them correctly rounded. */
+double tmo_logf_max_ulp(float lo, float hi, uint32_t stride, double *correct_share);
 
 /* Per-photon rand() stream (what the injected rand() returns). */
 typedef struct tmo_stream {

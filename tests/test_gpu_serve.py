@@ -1,6 +1,9 @@
 """The request server on the GPU: a request's result is the same alone and in
 a mix of concurrent requests, equals the plain kernel over the same photons,
-stops by its rule, and admission refuses requests when slots are full."""
+stops by its rule, and admission refuses requests when slots are full.  Each
+check runs on the three ways the server can drive the GPU: waves of the
+kernel with per-item barriers, waves of the barrier-free kernel, and the
+persistent launch fed from a work queue in mapped host memory."""
 import math
 
 import numpy as np
@@ -19,20 +22,25 @@ def req(mu_a=2.0, mu_s=20.0, shells=101, rse=0.02, cap=1 << 20, base=0):
     return r
 
 
+# server modes: waves of the kernel with per-item barriers, waves of the
+# barrier-free kernel, one persistent launch fed from a work queue
+MODES = {"waves_batch": dict(stream=0), "waves_stream": dict(stream=1), "persistent": dict(persistent=1)}
+OTHER = {"waves_batch": "persistent", "waves_stream": "waves_batch", "persistent": "waves_stream"}
+
 MIX = [req(2.0, 20.0, 101, 0.02, base=1 << 32), req(0.5, 50.0, 501, 0.03, base=2 << 32),
        req(5.0, 5.0, 101, 0.01, base=3 << 32), req(1.0, 300.0, 501, 0.05, base=4 << 32),
        req(0.02, 2.0, 101, 0.04, cap=1 << 16, base=5 << 32)]
 
 
-@pytest.mark.parametrize("stream", [0, 1])
-def test_alone_equals_in_mix(tmc_mod, stream):
+@pytest.mark.parametrize("mode", list(MODES))
+def test_alone_equals_in_mix(tmc_mod, mode):
     from tiny_mc_gb300.serve import Server
     probe = req(1.0, 30.0, 101, 0.02, base=9 << 32)
-    s = Server(slots=8, stream=1 - stream)      # alone on the other kernel
+    s = Server(slots=8, **MODES[OTHER[mode]])      # alone, driven the other way
     rid = s.submit(probe)
     alone = s.run({rid: 101})[rid]
     s.close()
-    s = Server(slots=8, stream=stream)
+    s = Server(slots=8, **MODES[mode])
     ids = {s.submit(r): int(r["shells"]) for r in MIX[:3]}
     rid = s.submit(probe)
     ids[rid] = 101
@@ -47,10 +55,10 @@ def test_alone_equals_in_mix(tmc_mod, stream):
     assert r_alone["rse"] == r_mix["rse"]
 
 
-@pytest.mark.parametrize("stream", [0, 1])
-def test_result_equals_plain_kernel_and_rule(tmc_mod, stream):
+@pytest.mark.parametrize("mode", list(MODES))
+def test_result_equals_plain_kernel_and_rule(tmc_mod, mode):
     from tiny_mc_gb300.serve import Server
-    s = Server(slots=8, stream=stream)
+    s = Server(slots=8, **MODES[mode])
     ids = {s.submit(r): int(r["shells"]) for r in MIX}
     out = s.run(ids)
     s.close()
@@ -73,15 +81,15 @@ def test_result_equals_plain_kernel_and_rule(tmc_mod, stream):
         assert b == cap_b or (b >= 16 and (b & (b - 1)) == 0)
 
 
-@pytest.mark.parametrize("stream", [0, 1])
-def test_item_split_does_not_change_results(tmc_mod, stream):
+@pytest.mark.parametrize("mode", list(MODES))
+def test_item_split_does_not_change_results(tmc_mod, mode):
     """RSE batches split into several work items (walked by different blocks),
     fewer launches in flight and a small in-flight item budget give the same
     tallies, steps, batch counts and RSE to the last bit."""
     from tiny_mc_gb300.serve import Server
     out = []
     for spi, waves, items in ((0.0, 0, 0), (float(1 << 16), 4, 64)):
-        s = Server(slots=8, stream=stream, steps_per_item=spi, waves=waves, inflight_items=items)
+        s = Server(slots=8, steps_per_item=spi, waves=waves, inflight_items=items, **MODES[mode])
         ids = {s.submit(r): int(r["shells"]) for r in MIX}
         out.append(s.run(ids))
         s.close()
@@ -107,11 +115,12 @@ def test_admission_refuses_when_full(tmc_mod):
     s.close()
 
 
-def test_run_trace_small(tmc_mod):
+@pytest.mark.parametrize("mode", list(MODES))
+def test_run_trace_small(tmc_mod, mode):
     from tiny_mc_gb300.serve import Server, make_trace
     req_, arr = make_trace(60, rate=400.0, seed=3, mu_a_range=(0.5, 10.0), mu_s_range=(1.0, 100.0),
                            rse=(0.02, 0.05), max_photons=1 << 18)
-    s = Server(slots=16)
+    s = Server(slots=16, **MODES[mode])
     res, done = s.run_trace(req_, arr, time_limit_s=120.0)
     assert done == 60
     assert np.all(res["latency_s"] > 0) and np.all(res["photons"] > 0)
@@ -120,8 +129,10 @@ def test_run_trace_small(tmc_mod):
     s.close()
 
 
-@pytest.mark.parametrize("stream,spi", [(0, 0.0), (1, 0.0), (0, float(1 << 24)), (1, float(1 << 22))])
-def test_rse_from_exact_batch_probes_with_wraps(tmc_mod, stream, spi):
+@pytest.mark.parametrize("mode,spi", [("waves_batch", 0.0), ("waves_stream", 0.0), ("persistent", 0.0),
+                                      ("waves_batch", float(1 << 24)), ("waves_stream", float(1 << 22)),
+                                      ("persistent", float(1 << 22))])
+def test_rse_from_exact_batch_probes_with_wraps(tmc_mod, mode, spi):
     """One shell and albedo 0.9999 with 2048-photon batches: each batch's sum
     of w in the probe shell (~2e7 weight units) exceeds 2^64 fixed-point
     units, so the per-item probe must count its wraps.  The server's RSE must
@@ -129,7 +140,7 @@ def test_rse_from_exact_batch_probes_with_wraps(tmc_mod, stream, spi):
     plain-kernel tallies of the same photons."""
     from tiny_mc_gb300.serve import Server
     r = req(mu_a=0.1, mu_s=1000.0, shells=1, rse=1e-9, cap=32 * 2048, base=77 << 32)
-    s = Server(slots=4, steps_per_batch=float(1 << 28), stream=stream, steps_per_item=spi)
+    s = Server(slots=4, steps_per_batch=float(1 << 28), steps_per_item=spi, **MODES[mode])
     rid = s.submit(r)
     tally, res = s.run({rid: 1})[rid]
     s.close()

@@ -58,7 +58,16 @@ def test_tmo_logf_accuracy(oracle_mod):
             assert v == 0.0
             continue
         worst = max(worst, abs(v - ref) / float(np.spacing(np.float32(abs(ref)))))
-    assert worst < 2.0
+    assert worst < 1.0
+
+
+def test_tmo_logf_accuracy_dense():
+    """Every 7th float of [2^-31, 1] (3.7e7 values; the whole range was
+    checked when the coefficients were chosen: max 0.86 ulp, 98.3% correctly
+    rounded)."""
+    from oracle import oracle
+    worst, share = oracle.logf_max_ulp(2.0 ** -31, 1.0, 7)
+    assert worst < 0.9 and share > 0.98, (worst, share)
 
 
 # ------------------------------------------- restatement vs reference photon.c

@@ -20,7 +20,7 @@ def test_trace_shape_and_rates():
 @pytest.mark.parametrize("field,value", [("slots", 0), ("max_shells", 0), ("min_batches", 1),
                                          ("block", 100), ("math", 9), ("max_items_per_request", 0),
                                          ("waves", 65), ("steps_per_item", -1.0),
-                                         ("steps_per_batch", 0.0)])
+                                         ("steps_per_batch", 0.0), ("persistent", 2)])
 def test_invalid_server_config_rejected(tmc_mod, field, value):
     from tiny_mc_gb300.serve import default_config
     c = default_config(**{field: value})
@@ -33,7 +33,8 @@ def test_default_server_config(tmc_mod):
     c = default_config()
     assert c.probe_shell == 10 and c.min_batches >= 2 and c.slots > 0
     assert c.waves == 0 and c.inflight_items == 0 and c.steps_per_item == 0.0   # 16, unbounded, unsplit
-    assert ctypes.sizeof(c) == 64
+    assert c.persistent in (0, 1)
+    assert ctypes.sizeof(c) == 72
 
 
 # ------------------------------------------------ the server's host-side plan

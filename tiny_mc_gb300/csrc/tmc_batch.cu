@@ -314,7 +314,7 @@ cudaError_t enqueue(const tmc_batch *b, cudaStream_t s)
         return e;
     // launch only (no attribute calls, so it can be captured): plan() has set
     // the kernel's shared-memory limit and the resident grid
-    BatchArgs a;
+    BatchArgs a{};
     a.keys = make_philox_keys(b->seed);
     a.problems = b->d_problems;
     a.items = b->d_items;

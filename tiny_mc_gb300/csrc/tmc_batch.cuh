@@ -11,6 +11,9 @@ namespace tmc {
 
 constexpr int BATCH_CHUNK = 32;   // photon ids a warp claims from its item at once
 
+// The queue-mode control word (BatchArgs::q_mode), written by the host.
+constexpr unsigned QUEUE_HOLD = 0, QUEUE_DRAIN = 1, QUEUE_STOP = 2;
+
 struct BatchProblemDev {
     WalkConsts c;
     unsigned long long id_base;
@@ -46,6 +49,23 @@ struct BatchArgs {
     // items' buffers are not freed, so waiting warps run into the limit.
     unsigned long long wait_limit_ns;
     const unsigned *hold_buffers;
+    // Queue mode of walk_stream (the request server's persistent launch),
+    // when q_items is not null: the items are a ring of q_cap entries (a power
+    // of two) in mapped host memory that the host keeps filling while the
+    // kernel runs, and `problems` is mapped host memory too.  *q_published
+    // (host-written, release) counts the items published so far and
+    // *item_counter (device) those claimed; a block claims only published
+    // items, and item i's completion goes to done_ring entry i % q_cap with i
+    // in its third word.  *q_mode (host-written) says what a block does when
+    // nothing is published: QUEUE_HOLD waits (up to the wait limit),
+    // QUEUE_DRAIN ends after idle_limit_ns, QUEUE_STOP ends at once.
+    // *q_live (device) counts the blocks still running.
+    const BatchItemDev *q_items;
+    const unsigned long long *q_published;
+    const unsigned *q_mode;
+    unsigned *q_live;
+    uint32_t q_cap;
+    unsigned long long idle_limit_ns;
 };
 
 // Publish a finished item into the completion ring (one thread).  The
@@ -65,6 +85,18 @@ __device__ __forceinline__ void publish_item(const BatchArgs &a, uint32_t it, un
     e[3] = 1ull;
 }
 
+// Queue mode: the completion of queue item `index` into its own ring entry.
+__device__ __forceinline__ void publish_item_at(const BatchArgs &a, unsigned long long index,
+                                                unsigned long long lo, unsigned long long hi)
+{
+    volatile unsigned long long *e = a.done_ring + 4 * (size_t)(index & (a.q_cap - 1));
+    e[0] = lo;
+    e[1] = hi;
+    e[2] = index;
+    __threadfence_system();
+    e[3] = 1ull;
+}
+
 size_t walk_batch_smem(uint32_t max_shells, int block);
 // Sets the kernel's shared-memory limit and returns the resident grid.
 cudaError_t walk_batch_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid);
@@ -73,7 +105,10 @@ cudaError_t walk_batch_launch(const BatchArgs &a, int block, uint32_t math, int 
 
 // The barrier-free variant (tmc_stream.cu): up to two items open per block.
 size_t walk_stream_smem(uint32_t max_shells, int block);
-cudaError_t walk_stream_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid);
+// Sets the shared-memory limit of the list form (queue = false) or the queue
+// form and returns its resident grid.
+cudaError_t walk_stream_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid,
+                                bool queue = false);
 cudaError_t walk_stream_launch(const BatchArgs &a, int block, uint32_t math, int grid, cudaStream_t s);
 
 }  // namespace tmc

@@ -86,30 +86,34 @@ __device__ __forceinline__ float uniform_pm1(uint32_t word)
 }
 
 // ------------------------------------------------------------ arithmetic
-// The library's logarithm for TMC_MATH_EXACT: x = 2^k m, m in
-// [sqrt(1/2), sqrt(2)); log(m) = 2 atanh(s), s = (m-1)/(m+1), odd Taylor
-// series of atanh through s^9; log x = k ln2_hi + (k ln2_lo + log m).  Each
-// step is one IEEE-rounded float operation (no contraction), so the CPU
-// restatement reproduces it bit for bit.  Max error about 1.6 ulp on
-// [2^-31, 1].
+// The library's logarithm for TMC_MATH_EXACT, division-free: x = 2^k m with
+// m in [sqrt(1/2), sqrt(2)), f = m - 1 (exact), log(m) = f + f^2 R(f) with R
+// a degree-8 polynomial (the Chebyshev interpolant of log1p(f)/f at 10 nodes
+// on [sqrt(1/2)-1, sqrt(2)-1], coefficients rounded to float; oracle/logfit.py
+// derives them), evaluated by Horner with fused multiply-adds, and log x =
+// k ln2_hi + (k ln2_lo + log m) with ln2 split so k ln2_hi is exact.  Every
+// step is one IEEE-rounded operation (fma rounds once), so the CPU
+// restatement reproduces it bit for bit.  Max error 0.86 ulp over every float
+// in [2^-31, 1] (98.3% correctly rounded).
 __device__ __forceinline__ float log_exact(float x)
 {
     const uint32_t ix = __float_as_uint(x);
     const int k = (int)((ix + 0x004afb0du) >> 23) - 127;
     const float m = __uint_as_float(ix - ((uint32_t)k << 23));
     const float f = __fsub_rn(m, 1.0f);
-    const float s = __fdiv_rn(f, __fadd_rn(2.0f, f));
-    const float z = __fmul_rn(s, s);
-    float pz = 0.222222222f;                          // 2/9
-    pz = __fadd_rn(__fmul_rn(pz, z), 0.285714286f);   // 2/7
-    pz = __fadd_rn(__fmul_rn(pz, z), 0.4f);           // 2/5
-    pz = __fadd_rn(__fmul_rn(pz, z), 0.666666667f);   // 2/3
-    const float tail = __fmul_rn(__fmul_rn(s, z), pz);
-    const float lm = __fadd_rn(__fadd_rn(s, s), tail);
-    const float kf = (float)k;
-    const float hi = __fmul_rn(kf, 0.693145751953125f);
-    const float lo = __fmul_rn(kf, 1.42860682e-6f);
-    return __fadd_rn(hi, __fadd_rn(lo, lm));
+    const float f2 = __fmul_rn(f, f);
+    float r = -0x1.31335ap-4f;
+    r = __fmaf_rn(r, f, 0x1.064786p-3f);
+    r = __fmaf_rn(r, f, -0x1.0fb036p-3f);
+    r = __fmaf_rn(r, f, 0x1.22cf10p-3f);
+    r = __fmaf_rn(r, f, -0x1.5423b0p-3f);
+    r = __fmaf_rn(r, f, 0x1.999e86p-3f);
+    r = __fmaf_rn(r, f, -0x1.000424p-2f);
+    r = __fmaf_rn(r, f, 0x1.55555ep-2f);
+    r = __fmaf_rn(r, f, -0x1.fffff8p-2f);
+    const float lm = __fmaf_rn(f2, r, f);
+    const float kf = __int2float_rn(k);
+    return __fmaf_rn(kf, 0.693145751953125f, __fmaf_rn(kf, 1.42860682e-6f, lm));
 }
 
 __device__ __forceinline__ float sqrt_approx(float x)

@@ -29,7 +29,14 @@
 //  * takes each item as soon as it finishes: the kernel appends the item's
 //    probe value to a completion ring in mapped host memory after a
 //    system-scope fence, so a request's decision waits for its own items, not
-//    for the slowest item of the launch they were in.
+//    for the slowest item of the launch they were in;
+//  * or, with `persistent`, keeps one long-running launch of the barrier-free
+//    kernel busy instead of launching waves: pending items are published
+//    (least attained service first) into a ring in mapped host memory that
+//    the kernel's blocks claim from as they free up, and each item's
+//    completion lands in its own ring entry.  The blocks wait for more work
+//    while requests are active and end once none are; the next admission
+//    launches the kernel again.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -92,6 +99,24 @@ struct Done {
     std::vector<tmc_tally> tally;
 };
 
+// The work queue of the persistent mode (mapped host memory unless noted).
+struct Queue {
+    uint32_t cap = 0;                          // ring entries, a power of two
+    BatchItemDev *h_items = nullptr, *d_items = nullptr;
+    unsigned long long *h_pub = nullptr, *d_pub = nullptr;   // items published
+    unsigned *h_mode = nullptr, *d_mode = nullptr;           // QUEUE_HOLD / DRAIN / STOP
+    unsigned long long *h_ring = nullptr, *d_ring = nullptr; // completions [cap][4]
+    BatchProblemDev *h_problems = nullptr, *d_problems = nullptr;
+    unsigned long long *d_counter = nullptr;   // device: claim counter, error flag, live blocks
+    uint64_t published = 0;                    // items published so far
+    uint64_t harvested = 0;                    // items below this index are all harvested
+    std::vector<uint64_t> req;                 // per entry: request id of the item
+    std::vector<uint64_t> g;                   // per entry: item index within its request
+    std::vector<uint8_t> state;                // per entry: 0 free, 1 published, 2 harvested
+    unsigned mode = QUEUE_DRAIN;
+    bool drained = true;                       // mode was DRAIN since the last launch
+};
+
 }  // namespace
 
 struct tmc_server {
@@ -113,6 +138,7 @@ struct tmc_server {
     uint64_t next_id = 1;
     uint64_t photons = 0, steps = 0, n_waves = 0;
     PhiloxKeys keys{};
+    Queue q;                                 // persistent mode
 };
 
 namespace {
@@ -121,6 +147,8 @@ void destroy_server(tmc_server *s)
 {
     if (!s)
         return;
+    if (s->q.h_mode)   // running persistent blocks finish their items and end
+        __atomic_store_n(s->q.h_mode, QUEUE_STOP, __ATOMIC_RELEASE);
     for (Wave &w : s->waves) {
         if (w.stream)
             cudaStreamSynchronize(w.stream);
@@ -136,6 +164,12 @@ void destroy_server(tmc_server *s)
     }
     if (s->admin)
         cudaStreamDestroy(s->admin);
+    cudaFreeHost(s->q.h_items);
+    cudaFreeHost(s->q.h_pub);
+    cudaFreeHost(s->q.h_mode);
+    cudaFreeHost(s->q.h_ring);
+    cudaFreeHost(s->q.h_problems);
+    cudaFree(s->q.d_counter);
     cudaFree(s->d_problems);
     cudaFree(s->d_tally);
     cudaFree(s->d_steps);
@@ -322,13 +356,14 @@ int harvest(tmc_server *s, Wave &w, bool ended)
     return TMC_OK;
 }
 
-// Fill a wave with pending items: least attained service first (requests
+// Take up to cap_n pending items: least attained service first (requests
 // with the fewest photon steps issued so far, i.e. new requests' first rounds,
 // go ahead of the later, larger rounds of long-running ones; ties in
-// admission order), at most `quota` items per request.
-int launch_wave(tmc_server *s, Wave &w)
+// admission order), at most `quota` items per request.  put(item, request id,
+// item index within the request) receives them in order.
+template <class Put>
+uint32_t take_pending(tmc_server *s, uint64_t cap_n, uint64_t quota_base, Put put)
 {
-    tmc::NvtxRange nvtx_range("tmc_server wave launch");
     uint32_t n = 0;
     std::vector<std::pair<double, uint64_t>> pend;
     for (uint64_t id : s->order) {
@@ -339,30 +374,42 @@ int launch_wave(tmc_server *s, Wave &w)
         if (q.issued < q.next_decision * q.items_per_batch)
             pend.push_back({(double)q.issued * q.item_photons * q.est_steps, id});
     }
-    if (pend.empty())
-        return TMC_OK;
+    if (pend.empty() || cap_n == 0)
+        return 0;
     const uint64_t quota = std::max<uint64_t>(
-        16, std::min<uint64_t>(s->cfg.max_items_per_request, s->wave_cap / pend.size()));
+        16, std::min<uint64_t>(s->cfg.max_items_per_request, quota_base / pend.size()));
     std::stable_sort(pend.begin(), pend.end(),
                      [](const auto &x, const auto &y) { return x.first < y.first; });
-    const uint64_t room = s->cfg.inflight_items
-                              ? (s->inflight < s->cfg.inflight_items ? s->cfg.inflight_items - s->inflight : 0)
-                              : ~0ull;
-    const uint64_t cap_n = std::min<uint64_t>(s->wave_cap, room);
     for (size_t c = 0; c < pend.size() && n < cap_n; ++c) {
         Req &q = s->active.find(pend[c].second)->second;   // present: collected above
         const uint64_t limit = q.next_decision * q.items_per_batch;
         const uint64_t k = std::min<uint64_t>({limit - q.issued, quota, cap_n - n});
         for (uint64_t j = 0; j < k; ++j) {
-            BatchItemDev &it = w.h_items[n++];
+            BatchItemDev it;
             it.problem = (uint32_t)q.slot;
             it.count = q.item_photons;
             it.first = (q.issued + j) * (uint64_t)q.item_photons;
+            put(it, q.id, q.issued + j);
+            ++n;
         }
         q.issued += k;
         if (q.probe.size() < 2 * q.issued)
             q.probe.resize(2 * q.issued, 0ull);
     }
+    return n;
+}
+
+// Fill a wave with pending items (take_pending's order) and launch it.
+int launch_wave(tmc_server *s, Wave &w)
+{
+    tmc::NvtxRange nvtx_range("tmc_server wave launch");
+    const uint64_t room = s->cfg.inflight_items
+                              ? (s->inflight < s->cfg.inflight_items ? s->cfg.inflight_items - s->inflight : 0)
+                              : ~0ull;
+    const uint64_t cap_n = std::min<uint64_t>(s->wave_cap, room);
+    uint32_t n = 0;
+    take_pending(s, cap_n, s->wave_cap,
+                 [&](const BatchItemDev &it, uint64_t, uint64_t) { w.h_items[n++] = it; });
     if (n == 0)
         return TMC_OK;
     w.n_items = n;
@@ -374,7 +421,7 @@ int launch_wave(tmc_server *s, Wave &w)
     if (e == cudaSuccess)   // item counter, error flag, ring tail
         e = cudaMemsetAsync(w.d_counter, 0, 3 * sizeof(unsigned long long), w.stream);
     if (e == cudaSuccess) {
-        BatchArgs a;
+        BatchArgs a{};
         a.keys = s->keys;
         a.problems = s->d_problems;
         a.items = w.d_items;
@@ -409,8 +456,162 @@ int launch_wave(tmc_server *s, Wave &w)
     return TMC_OK;
 }
 
+// ------------------------------------------------------- persistent mode
+
+// Take the finished queue items (any order), store their probes, decide.
+int harvest_queue(tmc_server *s)
+{
+    Queue &Q = s->q;
+    std::vector<uint64_t> touched;
+    for (uint64_t i = Q.harvested; i < Q.published; ++i) {
+        const uint32_t slot = (uint32_t)(i & (Q.cap - 1));
+        if (Q.state[slot] != 1)
+            continue;
+        unsigned long long *e = Q.h_ring + 4 * (size_t)slot;
+        if (__atomic_load_n(&e[3], __ATOMIC_ACQUIRE) == 0)
+            continue;
+        if (e[2] != i) {
+            set_error_text("server queue: completion entry for another item");
+            return TMC_E_STATE;
+        }
+        auto f = s->active.find(Q.req[slot]);
+        if (f == s->active.end() || 2 * Q.g[slot] + 1 >= f->second.probe.size()) {
+            set_error_text("server queue: a finished item matches no running request");
+            return TMC_E_STATE;
+        }
+        Req &q = f->second;
+        q.probe[2 * Q.g[slot]] = e[0];
+        q.probe[2 * Q.g[slot] + 1] = e[1];
+        ++q.done;
+        --s->inflight;
+        // the entry is free for item i + cap, which is published only after this
+        __atomic_store_n(&e[3], 0ull, __ATOMIC_RELAXED);
+        Q.state[slot] = 2;
+        touched.push_back(q.id);
+    }
+    while (Q.harvested < Q.published && Q.state[Q.harvested & (Q.cap - 1)] == 2) {
+        Q.state[Q.harvested & (Q.cap - 1)] = 0;
+        ++Q.harvested;
+    }
+    std::sort(touched.begin(), touched.end());
+    touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
+    for (uint64_t id : touched) {
+        int st = decide(s, id);
+        if (st)
+            return st;
+    }
+    return TMC_OK;
+}
+
+// Publish pending items into free ring entries, keeping at most
+// inflight_items published and unfinished (so a new request's first round
+// waits behind at most that many items), then release the new count.
+void publish_queue(tmc_server *s)
+{
+    Queue &Q = s->q;
+    const uint64_t budget = s->cfg.inflight_items ? s->cfg.inflight_items : 2ull * (uint64_t)s->grid;
+    const uint64_t room_ring = Q.cap - (Q.published - Q.harvested);
+    const uint64_t room = s->inflight < budget ? std::min<uint64_t>(budget - s->inflight, room_ring) : 0;
+    const uint32_t n = take_pending(s, room, budget, [&](const BatchItemDev &it, uint64_t id, uint64_t g) {
+        const uint64_t i = Q.published++;
+        const uint32_t slot = (uint32_t)(i & (Q.cap - 1));
+        Q.h_items[slot] = it;
+        Q.req[slot] = id;
+        Q.g[slot] = g;
+        Q.state[slot] = 1;
+    });
+    if (n) {
+        s->inflight += n;
+        __atomic_store_n(Q.h_pub, (unsigned long long)Q.published, __ATOMIC_RELEASE);
+    }
+}
+
+int launch_persistent(tmc_server *s, Wave &w)
+{
+    tmc::NvtxRange nvtx_range("tmc_server persistent launch");
+    Queue &Q = s->q;
+    BatchArgs a{};
+    a.keys = s->keys;
+    a.problems = Q.d_problems;
+    a.max_shells = s->cfg.max_shells;
+    a.probe_shell = s->cfg.probe_shell;
+    a.tally = s->d_tally;
+    a.steps = s->d_steps;
+    a.item_counter = Q.d_counter;
+    a.error = reinterpret_cast<unsigned *>(Q.d_counter + 1);
+    a.done_ring = Q.d_ring;
+    a.q_items = Q.d_items;
+    a.q_published = Q.d_pub;
+    a.q_mode = Q.d_mode;
+    a.q_live = reinterpret_cast<unsigned *>(Q.d_counter + 2);
+    a.q_cap = Q.cap;
+    a.idle_limit_ns = 20ull * 1000000ull;   // with no request active, blocks end after 20 ms
+    cudaError_t e = walk_stream_launch(a, (int)s->cfg.block, s->cfg.math, s->grid, w.stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(w.h_err, Q.d_counter + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                            w.stream);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(w.done, w.stream);
+    if (e != cudaSuccess)
+        return set_cuda_error(e, "server persistent launch");
+    w.busy = true;
+    w.n_items = 0;
+    ++s->n_waves;
+    Q.drained = false;
+    return TMC_OK;
+}
+
+int progress_persistent(tmc_server *s)
+{
+    Queue &Q = s->q;
+    uint32_t running = 0;
+    for (Wave &w : s->waves) {
+        if (!w.busy)
+            continue;
+        const cudaError_t e = cudaEventQuery(w.done);
+        if (e == cudaErrorNotReady) {
+            ++running;
+            continue;
+        }
+        if (e != cudaSuccess)
+            return set_cuda_error(e, "server persistent launch");
+        w.busy = false;
+        if (*w.h_err) {
+            set_error_text("server persistent launch: a bounded device wait ran out");
+            return TMC_E_TIMEOUT;
+        }
+    }
+    int st = harvest_queue(s);
+    if (st)
+        return st;
+    // blocks wait for work while requests are active, and end once none are
+    const unsigned mode = s->active.empty() ? QUEUE_DRAIN : QUEUE_HOLD;
+    if (mode != Q.mode) {
+        Q.mode = mode;
+        __atomic_store_n(Q.h_mode, mode, __ATOMIC_RELEASE);
+        if (mode == QUEUE_DRAIN)
+            Q.drained = true;
+    }
+    publish_queue(s);
+    // a launch is needed when work is queued and no launch runs, or when the
+    // running ones may be ending (the mode was DRAIN since they started)
+    if (Q.published > Q.harvested && (running == 0 || (Q.drained && mode == QUEUE_HOLD))) {
+        const uint32_t cap = s->cfg.waves ? s->cfg.waves : DEFAULT_WAVES;
+        for (Wave &w : s->waves) {
+            if (running >= cap)
+                break;
+            if (w.busy)
+                continue;
+            return launch_persistent(s, w);
+        }
+    }
+    return TMC_OK;
+}
+
 int progress_locked(tmc_server *s)
 {
+    if (s->cfg.persistent)
+        return progress_persistent(s);
     for (Wave &w : s->waves) {
         if (!w.busy)
             continue;
@@ -444,7 +645,7 @@ bool config_valid(const tmc_server_config &c)
            c.min_batches >= 2 && c.max_items_per_request > 0 && c.steps_per_batch > 0.0 &&
            c.steps_per_item >= 0.0 && c.waves <= (uint32_t)WAVES &&
            (c.math == TMC_MATH_EXACT || c.math == TMC_MATH_FAST) &&
-           (c.block == 128 || c.block == 256 || c.block == 512);
+           (c.block == 128 || c.block == 256 || c.block == 512) && c.persistent <= 1;
 }
 
 // The request's knobs as tmc_params checks them, plus the server's own limits.
@@ -499,6 +700,9 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
         return st;
     std::unique_ptr<tmc_server, void (*)(tmc_server *)> s(new tmc_server, destroy_server);
     s->cfg = *cfg;
+    if (cfg->persistent)
+        s->cfg.stream = 1;   // the queue form is the barrier-free kernel's
+    cfg = &s->cfg;
     s->device = c->device;
     s->sms = c->sms;
     s->keys = make_philox_keys(cfg->seed);
@@ -508,7 +712,8 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
         set_error_text("tmc_server_create: max_shells too large for the shared-memory histograms");
         return TMC_E_INVALID;
     }
-    cudaError_t e = cfg->stream ? walk_stream_prepare((int)cfg->block, cfg->math, cfg->max_shells, c->sms, &s->grid)
+    cudaError_t e = cfg->stream ? walk_stream_prepare((int)cfg->block, cfg->math, cfg->max_shells, c->sms, &s->grid,
+                                                      cfg->persistent != 0)
                                 : walk_batch_prepare((int)cfg->block, cfg->math, cfg->max_shells, c->sms, &s->grid);
     if (e != cudaSuccess)
         return set_cuda_error(e, "server kernel config");
@@ -540,6 +745,38 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
             e = cudaHostAlloc(&w.h_ring, 4 * sizeof(unsigned long long) * s->items_cap, cudaHostAllocMapped);
         if (e == cudaSuccess)
             e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&w.d_ring), w.h_ring, 0);
+    }
+    if (e == cudaSuccess && cfg->persistent) {
+        Queue &Q = s->q;
+        Q.cap = 1;
+        while (Q.cap < std::max<uint32_t>(4096, 4 * (uint32_t)s->grid))
+            Q.cap *= 2;
+        Q.req.assign(Q.cap, 0);
+        Q.g.assign(Q.cap, 0);
+        Q.state.assign(Q.cap, 0);
+        auto mapped = [&](auto **h, auto **d, size_t bytes) {
+            cudaError_t r = cudaHostAlloc(reinterpret_cast<void **>(h), bytes, cudaHostAllocMapped);
+            if (r == cudaSuccess) {
+                std::memset(*h, 0, bytes);
+                r = cudaHostGetDevicePointer(reinterpret_cast<void **>(d), *h, 0);
+            }
+            return r;
+        };
+        e = mapped(&Q.h_items, &Q.d_items, sizeof(BatchItemDev) * Q.cap);
+        if (e == cudaSuccess)
+            e = mapped(&Q.h_pub, &Q.d_pub, sizeof(unsigned long long));
+        if (e == cudaSuccess)
+            e = mapped(&Q.h_mode, &Q.d_mode, sizeof(unsigned));
+        if (e == cudaSuccess)
+            e = mapped(&Q.h_ring, &Q.d_ring, 4 * sizeof(unsigned long long) * Q.cap);
+        if (e == cudaSuccess)
+            e = mapped(&Q.h_problems, &Q.d_problems, sizeof(BatchProblemDev) * slots);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&Q.d_counter, 3 * sizeof(unsigned long long));
+        if (e == cudaSuccess)
+            e = cudaMemset(Q.d_counter, 0, 3 * sizeof(unsigned long long));
+        if (e == cudaSuccess)
+            *Q.h_mode = QUEUE_DRAIN;
     }
     if (e != cudaSuccess)
         return set_cuda_error(e, "tmc_server_create");
@@ -580,7 +817,11 @@ int tmc_server_submit(tmc_server *s, const tmc_request *r, uint64_t *id)
     pd.c.shells = q.d.shells;
     pd.id_base = r->photon_id_base;
     pd.tally_offset = (unsigned long long)q.slot * s->cfg.max_shells;
-    cudaError_t e = cudaMemcpyAsync(s->d_problems + q.slot, &pd, sizeof pd, cudaMemcpyHostToDevice, s->admin);
+    cudaError_t e = cudaSuccess;
+    if (s->cfg.persistent)   // read by the kernel only after the request's items are published
+        s->q.h_problems[q.slot] = pd;
+    else
+        e = cudaMemcpyAsync(s->d_problems + q.slot, &pd, sizeof pd, cudaMemcpyHostToDevice, s->admin);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(s->d_tally + 4ull * q.slot * s->cfg.max_shells, 0,
                             sizeof(tmc_tally) * s->cfg.max_shells, s->admin);

@@ -24,6 +24,14 @@
 //    bounded by wall time through %globaltimer (120 s unless the launch
 //    says otherwise): past the limit the warp sets the error flag and
 //    leaves; the host reports TMC_E_TIMEOUT.
+// Queue mode (the request server's persistent launch): the items come from a
+// ring in mapped host memory that the host keeps filling while the kernel
+// runs.  A block claims an item only once the host has published it (a
+// compare-and-swap on the claim counter below the published count, read with
+// acquire semantics), polls the published count with back-off when the ring
+// is empty, and ends when the host says stop, or says drain and nothing has
+// been published for the idle limit; while the host says hold, an empty ring
+// is waited on up to the wait limit.
 // Results are bit-identical to walk_batch and the plain kernel: the same
 // photons, integer sums.
 #include <algorithm>
@@ -51,6 +59,10 @@ struct __align__(16) OpenItem {    // per buffer, in shared memory
     WalkConsts c;                  // optics of the item's problem
     unsigned long long *g;         // the problem's 128-bit global tally
     unsigned long long id_first;   // photon id of the item's first photon
+    unsigned long long qidx;       // queue mode: the item's queue index
+    unsigned long long idle_since; // queue mode: first failed claim of this sequence (ns)
+    unsigned long long next_poll;  // queue mode: no poll of the published count before (ns)
+    uint32_t problem;              // the item's problem
     uint32_t item;                 // global item index, or END_ITEM
     uint32_t count;                // photons in the item
     uint32_t ps;                   // probe shell, clamped to the problem
@@ -62,20 +74,22 @@ struct __align__(16) OpenItem {    // per buffer, in shared memory
     uint32_t state;                // BUF_FREE / BUF_CLAIMING / BUF_OPEN
 };
 
-// Claim the next global item into buffer o (one thread).
-__device__ __forceinline__ void open_item(const BatchArgs &a, OpenItem *o)
+__device__ __forceinline__ unsigned long long load_acquire_sys(const unsigned long long *p)
 {
-    const unsigned long long it = atomicAdd(a.item_counter, 1ull);
-    o->item = it < a.n_items ? (uint32_t)it : END_ITEM;
-    if (it < a.n_items) {
-        const BatchItemDev itm = a.items[it];
-        const BatchProblemDev pr = a.problems[itm.problem];
-        o->c = pr.c;
-        o->g = a.tally + 4 * pr.tally_offset;
-        o->id_first = pr.id_base + itm.first;
-        o->count = itm.count;
-        o->ps = min(a.probe_shell, pr.c.shells - 1);
-    }
+    unsigned long long v;
+    asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void fill_item(const BatchArgs &a, OpenItem *o, const BatchItemDev &itm,
+                                          const BatchProblemDev &pr)
+{
+    o->c = pr.c;
+    o->g = a.tally + 4 * pr.tally_offset;
+    o->id_first = pr.id_base + itm.first;
+    o->count = itm.count;
+    o->problem = itm.problem;
+    o->ps = min(a.probe_shell, pr.c.shells - 1);
     o->next = 0;
     o->done = 0;
     o->wraps = 0;
@@ -83,9 +97,76 @@ __device__ __forceinline__ void open_item(const BatchArgs &a, OpenItem *o)
     o->steps_hi = 0;
 }
 
+// Claim the next item into buffer o (one thread).  Returns false only in
+// queue mode when nothing is published yet (try again later); otherwise o
+// holds the item, or END_ITEM when there is no more work.
+template <bool QUEUE>
+__device__ __forceinline__ bool open_item(const BatchArgs &a, OpenItem *o)
+{
+    if constexpr (!QUEUE) {
+        const unsigned long long it = atomicAdd(a.item_counter, 1ull);
+        o->item = it < a.n_items ? (uint32_t)it : END_ITEM;
+        if (it < a.n_items)
+            fill_item(a, o, a.items[it], a.problems[a.items[it].problem]);
+        return true;
+    }
+    const unsigned long long now = global_ns();
+    if (now < o->next_poll)
+        return false;
+    const unsigned long long pub = load_acquire_sys(a.q_published);
+    unsigned long long c = *(volatile unsigned long long *)a.item_counter;
+    while (c < pub) {
+        const unsigned long long prev = atomicCAS(a.item_counter, c, c + 1);
+        if (prev == c)
+            break;
+        c = prev;
+    }
+    if (c < pub) {
+        // the host wrote the item and its problem before publishing it
+        const volatile BatchItemDev *vi = a.q_items + (c & (a.q_cap - 1));
+        BatchItemDev itm;
+        itm.problem = vi->problem;
+        itm.count = vi->count;
+        itm.first = vi->first;
+        const volatile BatchProblemDev *vp = a.problems + itm.problem;
+        BatchProblemDev pr;
+        pr.c.albedo = vp->c.albedo;
+        pr.c.spm = vp->c.spm;
+        pr.c.last = vp->c.last;
+        pr.c.shells = vp->c.shells;
+        pr.id_base = vp->id_base;
+        pr.tally_offset = vp->tally_offset;
+        fill_item(a, o, itm, pr);
+        o->item = (uint32_t)(c & (a.q_cap - 1));
+        o->qidx = c;
+        o->idle_since = 0;
+        o->next_poll = 0;
+        return true;
+    }
+    const unsigned mode = *(volatile const unsigned *)a.q_mode;
+    if (mode == QUEUE_STOP) {
+        o->item = END_ITEM;
+        return true;
+    }
+    if (o->idle_since == 0)
+        o->idle_since = now;
+    const unsigned long long waited = now - o->idle_since;
+    if (mode == QUEUE_DRAIN && waited > a.idle_limit_ns) {
+        o->item = END_ITEM;
+        return true;
+    }
+    if (waited > (a.wait_limit_ns ? a.wait_limit_ns : DEFAULT_WAIT_LIMIT_NS)) {
+        atomicExch(a.error, 1u);
+        o->item = END_ITEM;
+        return true;
+    }
+    o->next_poll = now + 256ull + min(waited >> 4, 16384ull);
+    return false;
+}
+
 }  // namespace
 
-template <int BLOCK, class M>
+template <int BLOCK, class M, bool QUEUE>
 __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
 {
     constexpr unsigned NWARPS = BLOCK / 32;
@@ -99,7 +180,15 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
     for (uint32_t s = threadIdx.x; s < 2 * HS; s += BLOCK)
         smem[s] = 0;
     if (threadIdx.x == 0) {
-        open_item(a, &open[0]);
+        if (QUEUE && a.q_live)
+            atomicAdd(a.q_live, 1u);
+        for (int b = 0; b < 2; ++b) {
+            open[b].idle_since = 0;
+            open[b].next_poll = 0;
+        }
+        // queue mode: wait (bounded inside open_item) for the first item
+        while (!open_item<QUEUE>(a, &open[0]))
+            __nanosleep(256);
         open[0].gen = 0;
         open[0].state = BUF_OPEN;
         open[1].gen = 1;
@@ -121,6 +210,12 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
     float x = 0.f, y = 0.f, z = 0.f, u = 0.f, v = 0.f, w = 1.f, weight = 1.f;
     uint32_t lb = 0;                          // buffer of this lane's photon
     uint32_t steps = 0;                       // steps of this lane's photon
+    // the constants of this lane's photon's item, read from the buffer's
+    // record once when the photon starts (the record cannot change while
+    // the photon lives: its warp has not reported the item yet)
+    WalkConsts pc{};
+    unsigned long long *pg = nullptr;
+    uint32_t pps = 0;
     unsigned long long wait_start = 0;
 
     for (;;) {
@@ -160,7 +255,7 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
                     const unsigned long long st =
                         ((unsigned long long)vopen[rb].steps_hi << 32) | vopen[rb].steps_lo;
                     if (st)
-                        atomicAdd(&a.steps[a.items[it].problem], st);
+                        atomicAdd(&a.steps[vopen[rb].problem], st);
                     if (a.item_probe) {
                         a.item_probe[2 * (size_t)it] = probe_lo;
                         a.item_probe[2 * (size_t)it + 1] = probe_hi;
@@ -169,8 +264,12 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
                 if (a.done_ring) {
                     __threadfence();
                     __syncwarp();
-                    if (lane == 0)
-                        publish_item(a, it, probe_lo, probe_hi);
+                    if (lane == 0) {
+                        if constexpr (QUEUE)
+                            publish_item_at(a, vopen[rb].qidx, probe_lo, probe_hi);
+                        else
+                            publish_item(a, it, probe_lo, probe_hi);
+                    }
                 }
                 __syncwarp();
                 for (uint32_t s = lane; s < 4 * S; s += 32)
@@ -232,6 +331,9 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
                     weight = 1.f;
                     lb = cb;
                     steps = 0;
+                    pc = open[cb].c;
+                    pg = open[cb].g;
+                    pps = open[cb].ps;
                 }
                 cn += k;
                 need = __ballot_sync(FULL_MASK, want);
@@ -246,10 +348,10 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
                 st = vopen[nb].state;
                 if (st == BUF_FREE &&
                     atomicCAS((unsigned *)&open[nb].state, BUF_FREE, BUF_CLAIMING) == BUF_FREE) {
-                    open_item(a, &open[nb]);
+                    const bool got = open_item<QUEUE>(a, &open[nb]);
                     __threadfence_block();
-                    vopen[nb].state = BUF_OPEN;
-                    st = BUF_OPEN;
+                    st = got ? BUF_OPEN : BUF_FREE;   // queue empty: free again, retry later
+                    vopen[nb].state = st;
                 }
             }
             st = __shfl_sync(FULL_MASK, st, 0);
@@ -315,7 +417,6 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
         }
 
         if (alive && (prod - cur) >= 6u) {   // a short lane waits for the next refill
-            const OpenItem &o = open[lb];
             const uint32_t *rd = my + (cur & (RING - 1)) * BLOCK;
             if (!pending) {
                 // move, photon.c:21-24
@@ -327,16 +428,16 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
                 y = M::move(y, t, v);
                 z = M::move(z, t, w);
                 // absorb, photon.c:26-32
-                const WalkConsts c = o.c;
+                const WalkConsts c = pc;
                 const float rr = M::radius_shells(x, y, z, c.spm);
                 const uint32_t shell = __float2uint_rz(fminf(rr, c.last));
                 const uint32_t S = c.shells;
                 uint32_t *t0 = smem + lb * HS + shell;
-                unsigned long long *g = o.g;
+                unsigned long long *g = pg;
                 uint32_t lo, hi;
                 fx40_split(weight, lo, hi);
                 tally_add(t0, t0 + S, &g[4 * shell + 1], lo, hi,
-                          shell == o.ps ? (uint32_t *)&open[lb].wraps : nullptr);
+                          shell == pps ? (uint32_t *)&open[lb].wraps : nullptr);
                 fx40_split(__fmul_rn(weight, weight), lo, hi);
                 tally_add(t0 + 2 * S, t0 + 3 * S, &g[4 * shell + 3], lo, hi);
                 weight = M::mul(weight, c.albedo);
@@ -381,6 +482,10 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
             }
         }
     }
+    // every warp has left the loop (their waits are bounded)
+    __syncthreads();
+    if (QUEUE && threadIdx.x == 0 && a.q_live)
+        atomicSub(a.q_live, 1u);
 }
 
 size_t walk_stream_smem(uint32_t max_shells, int block)
@@ -388,10 +493,10 @@ size_t walk_stream_smem(uint32_t max_shells, int block)
     return (size_t)32 * max_shells + (size_t)4 * SLOTS * block;
 }
 
-template <int BLOCK, class M>
+template <int BLOCK, class M, bool QUEUE>
 static cudaError_t stream_config(int sms, size_t smem, int *grid)
 {
-    auto kern = walk_stream<BLOCK, M>;
+    auto kern = walk_stream<BLOCK, M, QUEUE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
@@ -405,18 +510,38 @@ static cudaError_t stream_config(int sms, size_t smem, int *grid)
     return cudaSuccess;
 }
 
-cudaError_t walk_stream_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid)
+template <bool QUEUE>
+static cudaError_t stream_prepare(int block, bool fast, size_t smem, int sms, int *grid)
+{
+    switch (block) {
+    case 128: return fast ? stream_config<128, FastMath, QUEUE>(sms, smem, grid)
+                          : stream_config<128, ExactMath, QUEUE>(sms, smem, grid);
+    case 256: return fast ? stream_config<256, FastMath, QUEUE>(sms, smem, grid)
+                          : stream_config<256, ExactMath, QUEUE>(sms, smem, grid);
+    case 512: return fast ? stream_config<512, FastMath, QUEUE>(sms, smem, grid)
+                          : stream_config<512, ExactMath, QUEUE>(sms, smem, grid);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t walk_stream_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid,
+                                bool queue)
 {
     const size_t smem = walk_stream_smem(max_shells, block);
     const bool fast = math == TMC_MATH_FAST;
-    switch (block) {
-    case 128: return fast ? stream_config<128, FastMath>(sms, smem, grid)
-                          : stream_config<128, ExactMath>(sms, smem, grid);
-    case 256: return fast ? stream_config<256, FastMath>(sms, smem, grid)
-                          : stream_config<256, ExactMath>(sms, smem, grid);
-    case 512: return fast ? stream_config<512, FastMath>(sms, smem, grid)
-                          : stream_config<512, ExactMath>(sms, smem, grid);
-    default: return cudaErrorInvalidValue;
+    return queue ? stream_prepare<true>(block, fast, smem, sms, grid)
+                 : stream_prepare<false>(block, fast, smem, sms, grid);
+}
+
+template <int BLOCK>
+static void stream_launch_b(const BatchArgs &a, bool fast, int grid, size_t smem, cudaStream_t s)
+{
+    if (a.q_items) {
+        if (fast) walk_stream<BLOCK, FastMath, true><<<grid, BLOCK, smem, s>>>(a);
+        else walk_stream<BLOCK, ExactMath, true><<<grid, BLOCK, smem, s>>>(a);
+    } else {
+        if (fast) walk_stream<BLOCK, FastMath, false><<<grid, BLOCK, smem, s>>>(a);
+        else walk_stream<BLOCK, ExactMath, false><<<grid, BLOCK, smem, s>>>(a);
     }
 }
 
@@ -425,20 +550,10 @@ cudaError_t walk_stream_launch(const BatchArgs &a, int block, uint32_t math, int
     const size_t smem = walk_stream_smem(a.max_shells, block);
     const bool fast = math == TMC_MATH_FAST;
     switch (block) {
-    case 128:
-        if (fast) walk_stream<128, FastMath><<<grid, 128, smem, s>>>(a);
-        else walk_stream<128, ExactMath><<<grid, 128, smem, s>>>(a);
-        break;
-    case 256:
-        if (fast) walk_stream<256, FastMath><<<grid, 256, smem, s>>>(a);
-        else walk_stream<256, ExactMath><<<grid, 256, smem, s>>>(a);
-        break;
-    case 512:
-        if (fast) walk_stream<512, FastMath><<<grid, 512, smem, s>>>(a);
-        else walk_stream<512, ExactMath><<<grid, 512, smem, s>>>(a);
-        break;
-    default:
-        return cudaErrorInvalidValue;
+    case 128: stream_launch_b<128>(a, fast, grid, smem, s); break;
+    case 256: stream_launch_b<256>(a, fast, grid, smem, s); break;
+    case 512: stream_launch_b<512>(a, fast, grid, smem, s); break;
+    default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }

@@ -29,7 +29,8 @@ class ServerConfig(ctypes.Structure):
                 ("seed", ctypes.c_uint64), ("math", ctypes.c_uint32), ("block", ctypes.c_uint32),
                 ("max_items_per_request", ctypes.c_uint32), ("stream", ctypes.c_uint32),
                 ("steps_per_batch", ctypes.c_double), ("steps_per_item", ctypes.c_double),
-                ("waves", ctypes.c_uint32), ("inflight_items", ctypes.c_uint32)]
+                ("waves", ctypes.c_uint32), ("inflight_items", ctypes.c_uint32),
+                ("persistent", ctypes.c_uint32)]
 
 
 def make_trace(n: int = 100000, rate: float = 2000.0, seed: int = 0, rse=(0.005, 0.05),
