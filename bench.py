@@ -64,15 +64,15 @@ NCU_WALK = {
     "capture": "profiles/walk_plain_fast_2p25photons_ncu_full.txt",
     "sources": ["tiny_mc_gb300/csrc/tmc_device.cuh", "tiny_mc_gb300/csrc/tmc_walk.cuh",
                 "tiny_mc_gb300/csrc/tmc_plain.cu"],
-    "sources_sha256": "9a865c5b49d40e40e681a31ca9d0d494bb7dc04ddd942aeb3f085e6d5ad9ba37",
+    "sources_sha256": "f012ddbaba91e908219599fc391eab0d801fd119d4ccd0f38ea35783ef404cff",
     # thread-instructions (predicated on) per photon step
     "thread_instr_per_step": 232.2,
     # busy fraction of each pipe
-    "pipes_busy": {"issue_slots": 0.815, "alu": 0.544, "fma_heavy": 0.489, "xu_sfu": 0.216,
+    "pipes_busy": {"issue_slots": 0.820, "alu": 0.544, "fma": 0.279, "xu_sfu": 0.109,
                    "shared_wavefronts": 0.515, "dram": 0.0},
-    # DRAM bytes read + written by one launch (the 101-shell tally flush only;
-    # not proportional to the photon count)
-    "dram_bytes_per_launch": 20736,
+    # DRAM bytes read + written by one launch (constant and code fetch plus the
+    # 101-shell tally flush; not proportional to the photon count)
+    "dram_bytes_per_launch": 85504,
 }
 
 
