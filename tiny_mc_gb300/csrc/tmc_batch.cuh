@@ -59,11 +59,17 @@ struct BatchArgs {
     // in its third word.  *q_mode (host-written) says what a block does when
     // nothing is published: QUEUE_HOLD waits (up to the wait limit),
     // QUEUE_DRAIN ends after idle_limit_ns, QUEUE_STOP ends at once.
-    // *q_live (device) counts the blocks still running.
+    // *q_live (device) counts the blocks still running.  Nothing is queued on
+    // the launch's stream behind the kernel (work waiting there could hold up
+    // other streams' copies in a shared hardware queue while the kernel waits
+    // for the host): the last block to end counts itself in *q_done_blocks
+    // (device, zero at launch) and writes {1, error flag} to q_ended (mapped).
     const BatchItemDev *q_items;
     const unsigned long long *q_published;
     const unsigned *q_mode;
     unsigned *q_live;
+    unsigned *q_done_blocks;
+    unsigned *q_ended;
     uint32_t q_cap;
     unsigned long long idle_limit_ns;
 };

@@ -108,6 +108,8 @@ struct Queue {
     unsigned long long *h_ring = nullptr, *d_ring = nullptr; // completions [cap][4]
     BatchProblemDev *h_problems = nullptr, *d_problems = nullptr;
     unsigned long long *d_counter = nullptr;   // device: claim counter, error flag, live blocks
+    unsigned *d_done = nullptr;                // device: per launch slot, blocks that ended
+    unsigned *h_end = nullptr, *d_end = nullptr;   // per launch slot: {ended, error}
     uint64_t published = 0;                    // items published so far
     uint64_t harvested = 0;                    // items below this index are all harvested
     std::vector<uint64_t> req;                 // per entry: request id of the item
@@ -170,6 +172,8 @@ void destroy_server(tmc_server *s)
     cudaFreeHost(s->q.h_ring);
     cudaFreeHost(s->q.h_problems);
     cudaFree(s->q.d_counter);
+    cudaFree(s->q.d_done);
+    cudaFreeHost(s->q.h_end);
     cudaFree(s->d_problems);
     cudaFree(s->d_tally);
     cudaFree(s->d_steps);
@@ -546,12 +550,15 @@ int launch_persistent(tmc_server *s, Wave &w)
     a.q_live = reinterpret_cast<unsigned *>(Q.d_counter + 2);
     a.q_cap = Q.cap;
     a.idle_limit_ns = 20ull * 1000000ull;   // with no request active, blocks end after 20 ms
-    cudaError_t e = walk_stream_launch(a, (int)s->cfg.block, s->cfg.math, s->grid, w.stream);
+    // the launch's end record; nothing goes on the stream after the kernel
+    const size_t k = (size_t)(&w - s->waves);
+    __atomic_store_n(&Q.h_end[2 * k], 0u, __ATOMIC_RELAXED);
+    Q.h_end[2 * k + 1] = 0u;
+    a.q_done_blocks = Q.d_done + k;
+    a.q_ended = Q.d_end + 2 * k;
+    cudaError_t e = cudaMemsetAsync(Q.d_done + k, 0, sizeof(unsigned), w.stream);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(w.h_err, Q.d_counter + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                            w.stream);
-    if (e == cudaSuccess)
-        e = cudaEventRecord(w.done, w.stream);
+        e = walk_stream_launch(a, (int)s->cfg.block, s->cfg.math, s->grid, w.stream);
     if (e != cudaSuccess)
         return set_cuda_error(e, "server persistent launch");
     w.busy = true;
@@ -568,15 +575,13 @@ int progress_persistent(tmc_server *s)
     for (Wave &w : s->waves) {
         if (!w.busy)
             continue;
-        const cudaError_t e = cudaEventQuery(w.done);
-        if (e == cudaErrorNotReady) {
+        const size_t k = (size_t)(&w - s->waves);
+        if (__atomic_load_n(&Q.h_end[2 * k], __ATOMIC_ACQUIRE) == 0) {
             ++running;
             continue;
         }
-        if (e != cudaSuccess)
-            return set_cuda_error(e, "server persistent launch");
         w.busy = false;
-        if (*w.h_err) {
+        if (Q.h_end[2 * k + 1]) {
             set_error_text("server persistent launch: a bounded device wait ran out");
             return TMC_E_TIMEOUT;
         }
@@ -771,6 +776,10 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
             e = mapped(&Q.h_ring, &Q.d_ring, 4 * sizeof(unsigned long long) * Q.cap);
         if (e == cudaSuccess)
             e = mapped(&Q.h_problems, &Q.d_problems, sizeof(BatchProblemDev) * slots);
+        if (e == cudaSuccess)
+            e = mapped(&Q.h_end, &Q.d_end, 2 * sizeof(unsigned) * WAVES);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&Q.d_done, sizeof(unsigned) * WAVES);
         if (e == cudaSuccess)
             e = cudaMalloc(&Q.d_counter, 3 * sizeof(unsigned long long));
         if (e == cudaSuccess)

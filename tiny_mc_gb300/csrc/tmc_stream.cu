@@ -484,8 +484,20 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
     }
     // every warp has left the loop (their waits are bounded)
     __syncthreads();
-    if (QUEUE && threadIdx.x == 0 && a.q_live)
-        atomicSub(a.q_live, 1u);
+    if (QUEUE && threadIdx.x == 0) {
+        if (a.q_live)
+            atomicSub(a.q_live, 1u);
+        // the launch's end record: written by its last block, after every
+        // block's flushes and completions (fenced before they counted)
+        __threadfence();
+        if (atomicAdd(a.q_done_blocks, 1u) == gridDim.x - 1) {
+            __threadfence();
+            volatile unsigned *e = a.q_ended;
+            e[1] = *(volatile const unsigned *)a.error;
+            __threadfence_system();
+            e[0] = 1u;
+        }
+    }
 }
 
 size_t walk_stream_smem(uint32_t max_shells, int block)
