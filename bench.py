@@ -769,8 +769,8 @@ def serve_leg(args, device_id):
     lat_o = res_o["latency_s"][got]
     s.close()
     s = Server(slots=args.serve_slots, math=math, **kw)
-    kernel = ("barrier-free, one persistent launch fed from a work queue" if s.cfg.persistent else
-              "barrier-free, waves of launches" if s.cfg.stream else "per-item barriers, waves of launches")
+    kernel = (("barrier-free" if s.cfg.stream else "per-item barriers") +
+              (", one persistent launch fed from a work queue" if s.cfg.persistent else ", waves of launches"))
     rate = 0.7 * saturated / mean_steps
     n3 = max(50, min(int(rate * args.serve_duration), n_total - C))
     sel3 = slice(C, C + n3)

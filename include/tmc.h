@@ -333,11 +333,12 @@ typedef struct tmc_server_config {
                                        long-running ones (0 = unbounded; with persistent,
                                        0 = twice the resident blocks) */
     uint32_t persistent;            /* 1: instead of launches per wave, a long-running
-                                       launch of the barrier-free kernel takes items from a
+                                       launch of the batched kernel (per-item barriers, or
+                                       barrier-free with stream = 1) takes items from a
                                        work queue in mapped host memory that the server
                                        keeps filling (least attained service first); its
                                        blocks wait for work while requests are active and
-                                       end once none are (waves and stream do not apply) */
+                                       end once none are (waves does not apply) */
 } tmc_server_config;
 
 typedef struct tmc_server tmc_server;

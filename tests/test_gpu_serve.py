@@ -1,9 +1,9 @@
 """The request server on the GPU: a request's result is the same alone and in
 a mix of concurrent requests, equals the plain kernel over the same photons,
 stops by its rule, and admission refuses requests when slots are full.  Each
-check runs on the three ways the server can drive the GPU: waves of the
-kernel with per-item barriers, waves of the barrier-free kernel, and the
-persistent launch fed from a work queue in mapped host memory."""
+check runs on the four ways the server can drive the GPU: waves of the
+kernel with per-item barriers or of the barrier-free kernel, and a
+persistent launch of either, fed from a work queue in mapped host memory."""
 import math
 
 import numpy as np
@@ -24,8 +24,10 @@ def req(mu_a=2.0, mu_s=20.0, shells=101, rse=0.02, cap=1 << 20, base=0):
 
 # server modes: waves of the kernel with per-item barriers, waves of the
 # barrier-free kernel, one persistent launch fed from a work queue
-MODES = {"waves_batch": dict(stream=0), "waves_stream": dict(stream=1), "persistent": dict(persistent=1)}
-OTHER = {"waves_batch": "persistent", "waves_stream": "waves_batch", "persistent": "waves_stream"}
+MODES = {"waves_batch": dict(stream=0), "waves_stream": dict(stream=1), "persistent": dict(persistent=1),
+         "persistent_stream": dict(persistent=1, stream=1)}
+OTHER = {"waves_batch": "persistent", "waves_stream": "waves_batch", "persistent": "persistent_stream",
+         "persistent_stream": "waves_stream"}
 
 MIX = [req(2.0, 20.0, 101, 0.02, base=1 << 32), req(0.5, 50.0, 501, 0.03, base=2 << 32),
        req(5.0, 5.0, 101, 0.01, base=3 << 32), req(1.0, 300.0, 501, 0.05, base=4 << 32),
@@ -130,8 +132,9 @@ def test_run_trace_small(tmc_mod, mode):
 
 
 @pytest.mark.parametrize("mode,spi", [("waves_batch", 0.0), ("waves_stream", 0.0), ("persistent", 0.0),
-                                      ("waves_batch", float(1 << 24)), ("waves_stream", float(1 << 22)),
-                                      ("persistent", float(1 << 22))])
+                                      ("persistent_stream", 0.0), ("waves_batch", float(1 << 24)),
+                                      ("waves_stream", float(1 << 22)), ("persistent", float(1 << 24)),
+                                      ("persistent_stream", float(1 << 22))])
 def test_rse_from_exact_batch_probes_with_wraps(tmc_mod, mode, spi):
     """One shell and albedo 0.9999 with 2048-photon batches: each batch's sum
     of w in the probe shell (~2e7 weight units) exceeds 2^64 fixed-point

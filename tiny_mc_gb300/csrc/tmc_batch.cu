@@ -32,25 +32,58 @@
 
 namespace tmc {
 
-template <int BLOCK, class M>
+// QUEUE: the request server's persistent launch (BatchArgs, queue mode):
+// thread 0 claims each item from the ring in mapped host memory, waiting with
+// back-off while nothing is published (bounded: see queue_idle_verdict), and
+// each finished item's completion goes to the ring entry of its own index.
+template <int BLOCK, class M, bool QUEUE>
 __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
 {
+    constexpr uint32_t END = 0xffffffffu;
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ uint32_t sh_item, sh_next, sh_probe_wraps;
+    __shared__ BatchItemDev sh_itm;
+    __shared__ BatchProblemDev sh_pr;
+    __shared__ unsigned long long sh_qidx;
     uint32_t *my = smem + 4 * a.max_shells + threadIdx.x;
+    if (QUEUE && threadIdx.x == 0 && a.q_live)
+        atomicAdd(a.q_live, 1u);
 
     for (;;) {
         if (threadIdx.x == 0) {
-            sh_item = (uint32_t)min(atomicAdd(a.item_counter, 1ull), 0xffffffffull);
+            if constexpr (QUEUE) {
+                unsigned long long idle_since = 0;
+                sh_item = END;
+                for (;;) {
+                    BatchItemDev itm;
+                    BatchProblemDev pr;
+                    unsigned long long c = 0;
+                    if (queue_try_claim(a, itm, pr, c)) {
+                        sh_itm = itm;
+                        sh_pr = pr;
+                        sh_qidx = c;
+                        sh_item = (uint32_t)(c & (a.q_cap - 1));
+                        break;
+                    }
+                    const unsigned long long now = global_ns();
+                    if (idle_since == 0)
+                        idle_since = now;
+                    if (queue_idle_verdict(a, now - idle_since))
+                        break;
+                    __nanosleep(256u + (unsigned)min((now - idle_since) >> 4, 16384ull));
+                }
+            } else {
+                sh_item = (uint32_t)min(atomicAdd(a.item_counter, 1ull), 0xffffffffull);
+            }
             sh_next = 0;
             sh_probe_wraps = 0;
         }
         __syncthreads();
         const uint32_t it = sh_item;
-        if (it >= a.n_items)
+        if (QUEUE ? it == END : it >= a.n_items)
             break;
-        const BatchItemDev item = a.items[it];
-        const BatchProblemDev pr = a.problems[item.problem];
+        const BatchItemDev item = QUEUE ? sh_itm : a.items[it];
+        const BatchProblemDev pr = QUEUE ? sh_pr : a.problems[item.problem];
         const uint32_t S = pr.c.shells;
         for (uint32_t s = threadIdx.x; s < 4 * S; s += BLOCK)
             smem[s] = 0;
@@ -81,15 +114,21 @@ __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
         if (a.done_ring)
             __threadfence();
         __syncthreads();
-        if (a.done_ring && threadIdx.x == 0)
-            publish_item(a, it, probe_lo, sh_probe_wraps);
+        if (a.done_ring && threadIdx.x == 0) {
+            if constexpr (QUEUE)
+                publish_item_at(a, sh_qidx, probe_lo, sh_probe_wraps);
+            else
+                publish_item(a, it, probe_lo, sh_probe_wraps);
+        }
     }
+    if (QUEUE && threadIdx.x == 0)
+        queue_block_end(a);
 }
 
-template <int BLOCK, class M>
+template <int BLOCK, class M, bool QUEUE>
 static cudaError_t walk_batch_config(int sms, size_t smem, int *grid)
 {
-    auto kern = walk_batch<BLOCK, M>;
+    auto kern = walk_batch<BLOCK, M, QUEUE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
@@ -108,18 +147,37 @@ size_t walk_batch_smem(uint32_t max_shells, int block)
     return (size_t)16 * max_shells + (size_t)4 * SLOTS * block;
 }
 
-cudaError_t walk_batch_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid)
+template <bool QUEUE>
+static cudaError_t batch_prepare(int block, bool fast, size_t smem, int sms, int *grid)
+{
+    switch (block) {
+    case 128: return fast ? walk_batch_config<128, FastMath, QUEUE>(sms, smem, grid)
+                          : walk_batch_config<128, ExactMath, QUEUE>(sms, smem, grid);
+    case 256: return fast ? walk_batch_config<256, FastMath, QUEUE>(sms, smem, grid)
+                          : walk_batch_config<256, ExactMath, QUEUE>(sms, smem, grid);
+    case 512: return fast ? walk_batch_config<512, FastMath, QUEUE>(sms, smem, grid)
+                          : walk_batch_config<512, ExactMath, QUEUE>(sms, smem, grid);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t walk_batch_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid, bool queue)
 {
     const size_t smem = walk_batch_smem(max_shells, block);
     const bool fast = math == TMC_MATH_FAST;
-    switch (block) {
-    case 128: return fast ? walk_batch_config<128, FastMath>(sms, smem, grid)
-                          : walk_batch_config<128, ExactMath>(sms, smem, grid);
-    case 256: return fast ? walk_batch_config<256, FastMath>(sms, smem, grid)
-                          : walk_batch_config<256, ExactMath>(sms, smem, grid);
-    case 512: return fast ? walk_batch_config<512, FastMath>(sms, smem, grid)
-                          : walk_batch_config<512, ExactMath>(sms, smem, grid);
-    default: return cudaErrorInvalidValue;
+    return queue ? batch_prepare<true>(block, fast, smem, sms, grid)
+                 : batch_prepare<false>(block, fast, smem, sms, grid);
+}
+
+template <int BLOCK>
+static void batch_launch_b(const BatchArgs &a, bool fast, int grid, size_t smem, cudaStream_t s)
+{
+    if (a.q_items) {
+        if (fast) walk_batch<BLOCK, FastMath, true><<<grid, BLOCK, smem, s>>>(a);
+        else walk_batch<BLOCK, ExactMath, true><<<grid, BLOCK, smem, s>>>(a);
+    } else {
+        if (fast) walk_batch<BLOCK, FastMath, false><<<grid, BLOCK, smem, s>>>(a);
+        else walk_batch<BLOCK, ExactMath, false><<<grid, BLOCK, smem, s>>>(a);
     }
 }
 
@@ -128,20 +186,10 @@ cudaError_t walk_batch_launch(const BatchArgs &a, int block, uint32_t math, int 
     const size_t smem = walk_batch_smem(a.max_shells, block);
     const bool fast = math == TMC_MATH_FAST;
     switch (block) {
-    case 128:
-        if (fast) walk_batch<128, FastMath><<<grid, 128, smem, s>>>(a);
-        else walk_batch<128, ExactMath><<<grid, 128, smem, s>>>(a);
-        break;
-    case 256:
-        if (fast) walk_batch<256, FastMath><<<grid, 256, smem, s>>>(a);
-        else walk_batch<256, ExactMath><<<grid, 256, smem, s>>>(a);
-        break;
-    case 512:
-        if (fast) walk_batch<512, FastMath><<<grid, 512, smem, s>>>(a);
-        else walk_batch<512, ExactMath><<<grid, 512, smem, s>>>(a);
-        break;
-    default:
-        return cudaErrorInvalidValue;
+    case 128: batch_launch_b<128>(a, fast, grid, smem, s); break;
+    case 256: batch_launch_b<256>(a, fast, grid, smem, s); break;
+    case 512: batch_launch_b<512>(a, fast, grid, smem, s); break;
+    default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }

@@ -103,9 +103,93 @@ __device__ __forceinline__ void publish_item_at(const BatchArgs &a, unsigned lon
     e[3] = 1ull;
 }
 
+// -------------------------------------------- queue mode (persistent server)
+constexpr unsigned long long QUEUE_DEFAULT_WAIT_LIMIT_NS = 120ull * 1000000000ull;
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned long long load_acquire_sys(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Claim the next published queue item, if any (one thread): a compare-and-
+// swap on the claim counter below the published count, then the item and its
+// problem read from mapped host memory (written by the host before it
+// published the item).  Returns false when nothing is published.
+__device__ __forceinline__ bool queue_try_claim(const BatchArgs &a, BatchItemDev &itm, BatchProblemDev &pr,
+                                                unsigned long long &qidx)
+{
+    const unsigned long long pub = load_acquire_sys(a.q_published);
+    unsigned long long c = *(volatile unsigned long long *)a.item_counter;
+    while (c < pub) {
+        const unsigned long long prev = atomicCAS(a.item_counter, c, c + 1);
+        if (prev == c)
+            break;
+        c = prev;
+    }
+    if (c >= pub)
+        return false;
+    const volatile BatchItemDev *vi = a.q_items + (c & (a.q_cap - 1));
+    itm.problem = vi->problem;
+    itm.count = vi->count;
+    itm.first = vi->first;
+    const volatile BatchProblemDev *vp = a.problems + itm.problem;
+    pr.c.albedo = vp->c.albedo;
+    pr.c.spm = vp->c.spm;
+    pr.c.last = vp->c.last;
+    pr.c.shells = vp->c.shells;
+    pr.id_base = vp->id_base;
+    pr.tally_offset = vp->tally_offset;
+    qidx = c;
+    return true;
+}
+
+// What a block with nothing claimed does after waiting `waited` ns (one
+// thread): 1 = end (STOP, or DRAIN past the idle limit), 2 = end with the
+// error flag set (the wait limit ran out), 0 = keep waiting.
+__device__ __forceinline__ int queue_idle_verdict(const BatchArgs &a, unsigned long long waited)
+{
+    const unsigned mode = *(volatile const unsigned *)a.q_mode;
+    if (mode == QUEUE_STOP)
+        return 1;
+    if (mode == QUEUE_DRAIN && waited > a.idle_limit_ns)
+        return 1;
+    if (waited > (a.wait_limit_ns ? a.wait_limit_ns : QUEUE_DEFAULT_WAIT_LIMIT_NS)) {
+        atomicExch(a.error, 1u);
+        return 2;
+    }
+    return 0;
+}
+
+// The end of a queue-mode block (thread 0, after the block's last flush):
+// count the block out, and the launch's last block writes the end record.
+__device__ __forceinline__ void queue_block_end(const BatchArgs &a)
+{
+    if (a.q_live)
+        atomicSub(a.q_live, 1u);
+    __threadfence();
+    if (atomicAdd(a.q_done_blocks, 1u) == gridDim.x - 1) {
+        __threadfence();
+        volatile unsigned *e = a.q_ended;
+        e[1] = *(volatile const unsigned *)a.error;
+        __threadfence_system();
+        e[0] = 1u;
+    }
+}
+
 size_t walk_batch_smem(uint32_t max_shells, int block);
-// Sets the kernel's shared-memory limit and returns the resident grid.
-cudaError_t walk_batch_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid);
+// Sets the shared-memory limit of the list form (queue = false) or the queue
+// form and returns its resident grid.
+cudaError_t walk_batch_prepare(int block, uint32_t math, uint32_t max_shells, int sms, int *grid,
+                               bool queue = false);
 // Launch only (capturable); walk_batch_prepare must have run for this shape.
 cudaError_t walk_batch_launch(const BatchArgs &a, int block, uint32_t math, int grid, cudaStream_t s);
 

@@ -30,8 +30,8 @@
 //    probe value to a completion ring in mapped host memory after a
 //    system-scope fence, so a request's decision waits for its own items, not
 //    for the slowest item of the launch they were in;
-//  * or, with `persistent`, keeps one long-running launch of the barrier-free
-//    kernel busy instead of launching waves: pending items are published
+//  * or, with `persistent`, keeps one long-running launch of the batched
+//    kernel (either form) busy instead of launching waves: pending items are published
 //    (least attained service first) into a ring in mapped host memory that
 //    the kernel's blocks claim from as they free up, and each item's
 //    completion lands in its own ring entry.  The blocks wait for more work
@@ -141,6 +141,10 @@ struct tmc_server {
     uint64_t photons = 0, steps = 0, n_waves = 0;
     PhiloxKeys keys{};
     Queue q;                                 // persistent mode
+    // pinned zeros: a new request's device tally is cleared by a copy from
+    // here, which runs on a copy engine; a memset kernel could wait for SM
+    // room that the persistent launch's waiting blocks hold
+    unsigned char *h_zero = nullptr;
 };
 
 namespace {
@@ -166,6 +170,7 @@ void destroy_server(tmc_server *s)
     }
     if (s->admin)
         cudaStreamDestroy(s->admin);
+    cudaFreeHost(s->h_zero);
     cudaFreeHost(s->q.h_items);
     cudaFreeHost(s->q.h_pub);
     cudaFreeHost(s->q.h_mode);
@@ -556,9 +561,10 @@ int launch_persistent(tmc_server *s, Wave &w)
     Q.h_end[2 * k + 1] = 0u;
     a.q_done_blocks = Q.d_done + k;
     a.q_ended = Q.d_end + 2 * k;
-    cudaError_t e = cudaMemsetAsync(Q.d_done + k, 0, sizeof(unsigned), w.stream);
+    cudaError_t e = cudaMemcpyAsync(Q.d_done + k, s->h_zero, sizeof(unsigned), cudaMemcpyHostToDevice, w.stream);
     if (e == cudaSuccess)
-        e = walk_stream_launch(a, (int)s->cfg.block, s->cfg.math, s->grid, w.stream);
+        e = s->cfg.stream ? walk_stream_launch(a, (int)s->cfg.block, s->cfg.math, s->grid, w.stream)
+                          : walk_batch_launch(a, (int)s->cfg.block, s->cfg.math, s->grid, w.stream);
     if (e != cudaSuccess)
         return set_cuda_error(e, "server persistent launch");
     w.busy = true;
@@ -705,8 +711,6 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
         return st;
     std::unique_ptr<tmc_server, void (*)(tmc_server *)> s(new tmc_server, destroy_server);
     s->cfg = *cfg;
-    if (cfg->persistent)
-        s->cfg.stream = 1;   // the queue form is the barrier-free kernel's
     cfg = &s->cfg;
     s->device = c->device;
     s->sms = c->sms;
@@ -719,7 +723,8 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
     }
     cudaError_t e = cfg->stream ? walk_stream_prepare((int)cfg->block, cfg->math, cfg->max_shells, c->sms, &s->grid,
                                                       cfg->persistent != 0)
-                                : walk_batch_prepare((int)cfg->block, cfg->math, cfg->max_shells, c->sms, &s->grid);
+                                : walk_batch_prepare((int)cfg->block, cfg->math, cfg->max_shells, c->sms, &s->grid,
+                                                     cfg->persistent != 0);
     if (e != cudaSuccess)
         return set_cuda_error(e, "server kernel config");
     const size_t slots = cfg->slots;
@@ -751,6 +756,10 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
         if (e == cudaSuccess)
             e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&w.d_ring), w.h_ring, 0);
     }
+    if (e == cudaSuccess)
+        e = cudaMallocHost(&s->h_zero, sizeof(tmc_tally) * cfg->max_shells);
+    if (e == cudaSuccess)
+        std::memset(s->h_zero, 0, sizeof(tmc_tally) * cfg->max_shells);
     if (e == cudaSuccess && cfg->persistent) {
         Queue &Q = s->q;
         Q.cap = 1;
@@ -832,10 +841,11 @@ int tmc_server_submit(tmc_server *s, const tmc_request *r, uint64_t *id)
     else
         e = cudaMemcpyAsync(s->d_problems + q.slot, &pd, sizeof pd, cudaMemcpyHostToDevice, s->admin);
     if (e == cudaSuccess)
-        e = cudaMemsetAsync(s->d_tally + 4ull * q.slot * s->cfg.max_shells, 0,
-                            sizeof(tmc_tally) * s->cfg.max_shells, s->admin);
+        e = cudaMemcpyAsync(s->d_tally + 4ull * q.slot * s->cfg.max_shells, s->h_zero,
+                            sizeof(tmc_tally) * s->cfg.max_shells, cudaMemcpyHostToDevice, s->admin);
     if (e == cudaSuccess)
-        e = cudaMemsetAsync(s->d_steps + q.slot, 0, sizeof(unsigned long long), s->admin);
+        e = cudaMemcpyAsync(s->d_steps + q.slot, s->h_zero, sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                            s->admin);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(s->admin);
     if (e != cudaSuccess)

@@ -45,15 +45,8 @@ namespace tmc {
 namespace {
 
 constexpr uint32_t END_ITEM = 0xffffffffu;
-constexpr unsigned long long DEFAULT_WAIT_LIMIT_NS = 120ull * 1000000000ull;
+constexpr unsigned long long DEFAULT_WAIT_LIMIT_NS = QUEUE_DEFAULT_WAIT_LIMIT_NS;
 constexpr uint32_t BUF_FREE = 0, BUF_CLAIMING = 1, BUF_OPEN = 2;
-
-__device__ __forceinline__ unsigned long long global_ns()
-{
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-    return t;
-}
 
 struct __align__(16) OpenItem {    // per buffer, in shared memory
     WalkConsts c;                  // optics of the item's problem
@@ -73,13 +66,6 @@ struct __align__(16) OpenItem {    // per buffer, in shared memory
     uint32_t gen;                  // item sequence number the buffer is for
     uint32_t state;                // BUF_FREE / BUF_CLAIMING / BUF_OPEN
 };
-
-__device__ __forceinline__ unsigned long long load_acquire_sys(const unsigned long long *p)
-{
-    unsigned long long v;
-    asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
 
 __device__ __forceinline__ void fill_item(const BatchArgs &a, OpenItem *o, const BatchItemDev &itm,
                                           const BatchProblemDev &pr)
@@ -113,29 +99,10 @@ __device__ __forceinline__ bool open_item(const BatchArgs &a, OpenItem *o)
     const unsigned long long now = global_ns();
     if (now < o->next_poll)
         return false;
-    const unsigned long long pub = load_acquire_sys(a.q_published);
-    unsigned long long c = *(volatile unsigned long long *)a.item_counter;
-    while (c < pub) {
-        const unsigned long long prev = atomicCAS(a.item_counter, c, c + 1);
-        if (prev == c)
-            break;
-        c = prev;
-    }
-    if (c < pub) {
-        // the host wrote the item and its problem before publishing it
-        const volatile BatchItemDev *vi = a.q_items + (c & (a.q_cap - 1));
-        BatchItemDev itm;
-        itm.problem = vi->problem;
-        itm.count = vi->count;
-        itm.first = vi->first;
-        const volatile BatchProblemDev *vp = a.problems + itm.problem;
-        BatchProblemDev pr;
-        pr.c.albedo = vp->c.albedo;
-        pr.c.spm = vp->c.spm;
-        pr.c.last = vp->c.last;
-        pr.c.shells = vp->c.shells;
-        pr.id_base = vp->id_base;
-        pr.tally_offset = vp->tally_offset;
+    BatchItemDev itm;
+    BatchProblemDev pr;
+    unsigned long long c = 0;
+    if (queue_try_claim(a, itm, pr, c)) {
         fill_item(a, o, itm, pr);
         o->item = (uint32_t)(c & (a.q_cap - 1));
         o->qidx = c;
@@ -143,20 +110,10 @@ __device__ __forceinline__ bool open_item(const BatchArgs &a, OpenItem *o)
         o->next_poll = 0;
         return true;
     }
-    const unsigned mode = *(volatile const unsigned *)a.q_mode;
-    if (mode == QUEUE_STOP) {
-        o->item = END_ITEM;
-        return true;
-    }
     if (o->idle_since == 0)
         o->idle_since = now;
     const unsigned long long waited = now - o->idle_since;
-    if (mode == QUEUE_DRAIN && waited > a.idle_limit_ns) {
-        o->item = END_ITEM;
-        return true;
-    }
-    if (waited > (a.wait_limit_ns ? a.wait_limit_ns : DEFAULT_WAIT_LIMIT_NS)) {
-        atomicExch(a.error, 1u);
+    if (queue_idle_verdict(a, waited)) {
         o->item = END_ITEM;
         return true;
     }
@@ -484,20 +441,8 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
     }
     // every warp has left the loop (their waits are bounded)
     __syncthreads();
-    if (QUEUE && threadIdx.x == 0) {
-        if (a.q_live)
-            atomicSub(a.q_live, 1u);
-        // the launch's end record: written by its last block, after every
-        // block's flushes and completions (fenced before they counted)
-        __threadfence();
-        if (atomicAdd(a.q_done_blocks, 1u) == gridDim.x - 1) {
-            __threadfence();
-            volatile unsigned *e = a.q_ended;
-            e[1] = *(volatile const unsigned *)a.error;
-            __threadfence_system();
-            e[0] = 1u;
-        }
-    }
+    if (QUEUE && threadIdx.x == 0)
+        queue_block_end(a);
 }
 
 size_t walk_stream_smem(uint32_t max_shells, int block)
