@@ -35,7 +35,7 @@ namespace tmc {
 // QUEUE: the request server's persistent launch (BatchArgs, queue mode):
 // thread 0 claims each item from the ring in mapped host memory, waiting with
 // back-off while nothing is published (bounded: see queue_idle_verdict), and
-// each finished item's completion goes to the ring entry of its own index.
+// each finished item's completion is appended to the completion ring.
 template <int BLOCK, class M, bool QUEUE>
 __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
 {

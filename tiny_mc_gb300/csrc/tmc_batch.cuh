@@ -55,8 +55,8 @@ struct BatchArgs {
     // kernel runs, and `problems` is mapped host memory too.  *q_published
     // (host-written, release) counts the items published so far and
     // *item_counter (device) those claimed; a block claims only published
-    // items, and item i's completion goes to done_ring entry i % q_cap with i
-    // in its third word.  *q_mode (host-written) says what a block does when
+    // items, and each finished item's completion is appended to done_ring
+    // (done_tail, device, counts them) with the item's index in its third word.  *q_mode (host-written) says what a block does when
     // nothing is published: QUEUE_HOLD waits (up to the wait limit),
     // QUEUE_DRAIN ends after idle_limit_ns, QUEUE_STOP ends at once.
     // *q_live (device) counts the blocks still running.  Nothing is queued on
@@ -91,11 +91,16 @@ __device__ __forceinline__ void publish_item(const BatchArgs &a, uint32_t it, un
     e[3] = 1ull;
 }
 
-// Queue mode: the completion of queue item `index` into its own ring entry.
+// Queue mode: the completion of queue item `index`, appended to the
+// completion ring in finishing order (entry done_tail % q_cap), so the host
+// reads only new completions.  The host keeps at most q_cap items published
+// and unfinished, and clears an entry before publishing the item whose
+// completion could reuse it.
 __device__ __forceinline__ void publish_item_at(const BatchArgs &a, unsigned long long index,
                                                 unsigned long long lo, unsigned long long hi)
 {
-    volatile unsigned long long *e = a.done_ring + 4 * (size_t)(index & (a.q_cap - 1));
+    const unsigned t = atomicAdd(a.done_tail, 1u);
+    volatile unsigned long long *e = a.done_ring + 4 * (size_t)(t & (a.q_cap - 1));
     e[0] = lo;
     e[1] = hi;
     e[2] = index;

@@ -33,8 +33,9 @@
 //  * or, with `persistent`, keeps one long-running launch of the batched
 //    kernel (either form) busy instead of launching waves: pending items are published
 //    (least attained service first) into a ring in mapped host memory that
-//    the kernel's blocks claim from as they free up, and each item's
-//    completion lands in its own ring entry.  The blocks wait for more work
+//    the kernel's blocks claim from as they free up, and finished items are
+//    appended to a completion ring the host reads from its head.  The blocks
+//    wait for more work
 //    while requests are active and end once none are; the next admission
 //    launches the kernel again.
 #include <algorithm>
@@ -107,7 +108,9 @@ struct Queue {
     unsigned *h_mode = nullptr, *d_mode = nullptr;           // QUEUE_HOLD / DRAIN / STOP
     unsigned long long *h_ring = nullptr, *d_ring = nullptr; // completions [cap][4]
     BatchProblemDev *h_problems = nullptr, *d_problems = nullptr;
-    unsigned long long *d_counter = nullptr;   // device: claim counter, error flag, live blocks
+    unsigned long long *d_counter = nullptr;   // device: claim counter, error flag, live blocks,
+                                               // completion count
+    uint64_t done_head = 0;                    // completions taken from the ring
     unsigned *d_done = nullptr;                // device: per launch slot, blocks that ended
     unsigned *h_end = nullptr, *d_end = nullptr;   // per launch slot: {ended, error}
     uint64_t published = 0;                    // items published so far
@@ -467,20 +470,20 @@ int launch_wave(tmc_server *s, Wave &w)
 
 // ------------------------------------------------------- persistent mode
 
-// Take the finished queue items (any order), store their probes, decide.
+// Take the finished queue items from the completion ring (in finishing
+// order: only new entries are read), store their probes, decide.
 int harvest_queue(tmc_server *s)
 {
     Queue &Q = s->q;
     std::vector<uint64_t> touched;
-    for (uint64_t i = Q.harvested; i < Q.published; ++i) {
-        const uint32_t slot = (uint32_t)(i & (Q.cap - 1));
-        if (Q.state[slot] != 1)
-            continue;
-        unsigned long long *e = Q.h_ring + 4 * (size_t)slot;
+    for (;;) {
+        unsigned long long *e = Q.h_ring + 4 * (size_t)(Q.done_head & (Q.cap - 1));
         if (__atomic_load_n(&e[3], __ATOMIC_ACQUIRE) == 0)
-            continue;
-        if (e[2] != i) {
-            set_error_text("server queue: completion entry for another item");
+            break;
+        const uint64_t i = e[2];
+        const uint32_t slot = (uint32_t)(i & (Q.cap - 1));
+        if (i < Q.harvested || i >= Q.published || Q.state[slot] != 1) {
+            set_error_text("server queue: completion entry for an item not in flight");
             return TMC_E_STATE;
         }
         auto f = s->active.find(Q.req[slot]);
@@ -493,8 +496,9 @@ int harvest_queue(tmc_server *s)
         q.probe[2 * Q.g[slot] + 1] = e[1];
         ++q.done;
         --s->inflight;
-        // the entry is free for item i + cap, which is published only after this
+        // free for a later completion, which comes only after more publishing
         __atomic_store_n(&e[3], 0ull, __ATOMIC_RELAXED);
+        ++Q.done_head;
         Q.state[slot] = 2;
         touched.push_back(q.id);
     }
@@ -553,6 +557,7 @@ int launch_persistent(tmc_server *s, Wave &w)
     a.q_published = Q.d_pub;
     a.q_mode = Q.d_mode;
     a.q_live = reinterpret_cast<unsigned *>(Q.d_counter + 2);
+    a.done_tail = reinterpret_cast<unsigned *>(Q.d_counter + 3);
     a.q_cap = Q.cap;
     a.idle_limit_ns = 20ull * 1000000ull;   // with no request active, blocks end after 20 ms
     // the launch's end record; nothing goes on the stream after the kernel
@@ -790,9 +795,9 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
         if (e == cudaSuccess)
             e = cudaMalloc(&Q.d_done, sizeof(unsigned) * WAVES);
         if (e == cudaSuccess)
-            e = cudaMalloc(&Q.d_counter, 3 * sizeof(unsigned long long));
+            e = cudaMalloc(&Q.d_counter, 4 * sizeof(unsigned long long));
         if (e == cudaSuccess)
-            e = cudaMemset(Q.d_counter, 0, 3 * sizeof(unsigned long long));
+            e = cudaMemset(Q.d_counter, 0, 4 * sizeof(unsigned long long));
         if (e == cudaSuccess)
             *Q.h_mode = QUEUE_DRAIN;
     }
