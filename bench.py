@@ -28,7 +28,8 @@ Beside it, on one GPU (the default run; --plain-only leaves them out):
   problem on a subsample of the problems;
 * serve: the request stream (continuous batching, RSE stopping): capacity,
   the load offered at 2000 requests/s, and p50/p99 latency at 70 % of the
-  capacity.
+  capacity; serve_persistent: the same with the server's persistent launch
+  fed from a work queue (its low-latency setting).
 
 Multi-GPU (torchrun): each rank walks its own 2^30 photons (ids offset by
 rank), no collective on the data path; weak scaling.  After the timed region
@@ -123,8 +124,8 @@ def parse():
                     help="server: 1 one persistent launch fed from a work queue, 0 waves of launches, "
                          "-1 library default")
     ap.add_argument("--serve-calib", type=int, default=256)
-    ap.add_argument("--serve-window", type=float, default=5.0)
-    ap.add_argument("--serve-duration", type=float, default=30.0)
+    ap.add_argument("--serve-window", type=float, default=10.0)
+    ap.add_argument("--serve-duration", type=float, default=25.0)
     ap.add_argument("--serve-drain", type=float, default=60.0)
     ap.add_argument("--sweep-scale", type=float, default=1.0 / 64,
                     help="photon-count multiplier of the sweep (1 = full size, ~3.3e13 steps)")
@@ -571,6 +572,12 @@ def run_ours(args):
         legs["high_albedo"] = high_albedo_leg(args, tmc, torch, sfu_peak, device_id)
         legs["sweep"] = sweep_leg(args, tmc, torch, device_id, plain_steps_per_s=steps_per_launch / per_launch_s)
         legs["serve"] = serve_leg(args, device_id)
+        # the same stream on the server's low-latency setting: one persistent
+        # launch fed from a work queue
+        if args.serve_persistent < 0:
+            args.serve_persistent = 1
+            legs["serve_persistent"] = serve_leg(args, device_id)
+            args.serve_persistent = -1
 
     if rank == 0:
         line = {
@@ -756,7 +763,7 @@ def serve_leg(args, device_id):
     calib_steps = float(res_c["photon_steps"].sum())
     mean_steps = calib_steps / max(1, done_c)
     W = args.serve_window
-    sel = slice(C, C + int(2000.0 * W * 1.2))
+    sel = slice(C, C + int(2000.0 * W * 1.5))
     a2 = arr[sel] - arr[sel][0]
     w0 = s.work()
     t0 = time.perf_counter()
