@@ -26,10 +26,11 @@ Beside it, on one GPU (the default run; --plain-only leaves them out):
 * sweep: 4096 independent problems in one persistent launch (autotuned,
   CUDA-graph replay) at 1/64 of the photon counts, against one launch per
   problem on a subsample of the problems;
-* serve: the request stream (continuous batching, RSE stopping): capacity,
-  the load offered at 2000 requests/s, and p50/p99 latency at 70 % of the
-  capacity; serve_persistent: the same with the server's persistent launch
-  fed from a work queue (its low-latency setting).
+* serve: the request stream (continuous batching, RSE stopping) on the
+  server's persistent launch fed from a work queue: capacity, the load
+  offered at 2000 requests/s, and p50/p99 latency at 70 % of the capacity;
+  serve_waves: the same on the server's default setting (waves of
+  launches, which leave SM room for other work between launches).
 
 Multi-GPU (torchrun): each rank walks its own 2^30 photons (ids offset by
 rank), no collective on the data path; weak scaling.  After the timed region
@@ -571,13 +572,16 @@ def run_ours(args):
     if extra_legs:
         legs["high_albedo"] = high_albedo_leg(args, tmc, torch, sfu_peak, device_id)
         legs["sweep"] = sweep_leg(args, tmc, torch, device_id, plain_steps_per_s=steps_per_launch / per_launch_s)
-        legs["serve"] = serve_leg(args, device_id)
-        # the same stream on the server's low-latency setting: one persistent
-        # launch fed from a work queue
         if args.serve_persistent < 0:
+            # one persistent launch fed from a work queue (the server's
+            # setting for a dedicated GPU), then the default waves of launches
             args.serve_persistent = 1
-            legs["serve_persistent"] = serve_leg(args, device_id)
+            legs["serve"] = serve_leg(args, device_id)
+            args.serve_persistent = 0
+            legs["serve_waves"] = serve_leg(args, device_id)
             args.serve_persistent = -1
+        else:
+            legs["serve"] = serve_leg(args, device_id)
 
     if rank == 0:
         line = {

@@ -338,7 +338,11 @@ typedef struct tmc_server_config {
                                        work queue in mapped host memory that the server
                                        keeps filling (least attained service first); its
                                        blocks wait for work while requests are active and
-                                       end once none are (waves does not apply) */
+                                       end once none are (waves does not apply).  Higher
+                                       capacity and lower latency than waves, but while
+                                       requests are active it holds the SMs: other work on
+                                       the GPU waits for it (the default, 0, leaves room
+                                       between launches) */
 } tmc_server_config;
 
 typedef struct tmc_server tmc_server;

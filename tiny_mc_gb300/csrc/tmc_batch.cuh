@@ -49,14 +49,16 @@ struct BatchArgs {
     // items' buffers are not freed, so waiting warps run into the limit.
     unsigned long long wait_limit_ns;
     const unsigned *hold_buffers;
-    // Queue mode of walk_stream (the request server's persistent launch),
-    // when q_items is not null: the items are a ring of q_cap entries (a power
-    // of two) in mapped host memory that the host keeps filling while the
-    // kernel runs, and `problems` is mapped host memory too.  *q_published
-    // (host-written, release) counts the items published so far and
+    // Queue mode (the request server's persistent launch), when q_items is
+    // not null: items sit in a pool of q_cap slots (a power of two) in mapped
+    // host memory, and the queue is a ring of 2 q_cap pool slot numbers
+    // (q_order) in publishing order that the host keeps filling while the
+    // kernel runs; `problems` is mapped host memory too.  *q_published
+    // (host-written, release) counts the positions published so far and
     // *item_counter (device) those claimed; a block claims only published
-    // items, and each finished item's completion is appended to done_ring
-    // (done_tail, device, counts them) with the item's index in its third word.  *q_mode (host-written) says what a block does when
+    // positions, and each finished item's completion is appended to done_ring
+    // (done_tail, device, counts them) with the item's pool slot in its third
+    // word.  *q_mode (host-written) says what a block does when
     // nothing is published: QUEUE_HOLD waits (up to the wait limit),
     // QUEUE_DRAIN ends after idle_limit_ns, QUEUE_STOP ends at once.
     // *q_live (device) counts the blocks still running.  Nothing is queued on
@@ -64,7 +66,8 @@ struct BatchArgs {
     // other streams' copies in a shared hardware queue while the kernel waits
     // for the host): the last block to end counts itself in *q_done_blocks
     // (device, zero at launch) and writes {1, error flag} to q_ended (mapped).
-    const BatchItemDev *q_items;
+    const BatchItemDev *q_items;        // the item pool [q_cap]
+    const uint32_t *q_order;            // queue: pool slot per position [2 q_cap]
     const unsigned long long *q_published;
     const unsigned *q_mode;
     unsigned *q_live;
@@ -91,7 +94,7 @@ __device__ __forceinline__ void publish_item(const BatchArgs &a, uint32_t it, un
     e[3] = 1ull;
 }
 
-// Queue mode: the completion of queue item `index`, appended to the
+// Queue mode: the completion of the item in pool slot `index`, appended to the
 // completion ring in finishing order (entry done_tail % q_cap), so the host
 // reads only new completions.  The host keeps at most q_cap items published
 // and unfinished, and clears an entry before publishing the item whose
@@ -125,16 +128,25 @@ __device__ __forceinline__ unsigned long long load_acquire_sys(const unsigned lo
     return v;
 }
 
-// Claim the next published queue item, if any (one thread): a compare-and-
-// swap on the claim counter below the published count, then the item and its
-// problem read from mapped host memory (written by the host before it
-// published the item).  Returns false when nothing is published.
+// Claim the next published queue position, if any (one thread): the
+// position's pool slot is read from mapped host memory (written by the host
+// before it published the position), then a compare-and-swap on the claim
+// counter below the published count takes the position.  Reading the slot
+// before the swap makes it valid when the swap succeeds: the host rewrites a
+// position's entry 2 q_cap positions later, only after at least q_cap items
+// claimed after it have finished.  The item and its problem are then read from
+// the pool slot, which stays the item's until its completion is harvested.
+// qidx receives the pool slot, which identifies the item's completion.
+// Returns false when nothing is published.
 __device__ __forceinline__ bool queue_try_claim(const BatchArgs &a, BatchItemDev &itm, BatchProblemDev &pr,
                                                 unsigned long long &qidx)
 {
     const unsigned long long pub = load_acquire_sys(a.q_published);
     unsigned long long c = *(volatile unsigned long long *)a.item_counter;
+    uint32_t slot = 0;
     while (c < pub) {
+        slot = *(const volatile uint32_t *)(a.q_order + (c & (2 * a.q_cap - 1)));
+        __threadfence();
         const unsigned long long prev = atomicCAS(a.item_counter, c, c + 1);
         if (prev == c)
             break;
@@ -142,7 +154,7 @@ __device__ __forceinline__ bool queue_try_claim(const BatchArgs &a, BatchItemDev
     }
     if (c >= pub)
         return false;
-    const volatile BatchItemDev *vi = a.q_items + (c & (a.q_cap - 1));
+    const volatile BatchItemDev *vi = a.q_items + slot;
     itm.problem = vi->problem;
     itm.count = vi->count;
     itm.first = vi->first;
@@ -153,7 +165,7 @@ __device__ __forceinline__ bool queue_try_claim(const BatchArgs &a, BatchItemDev
     pr.c.shells = vp->c.shells;
     pr.id_base = vp->id_base;
     pr.tally_offset = vp->tally_offset;
-    qidx = c;
+    qidx = slot;
     return true;
 }
 

@@ -101,23 +101,27 @@ struct Done {
 };
 
 // The work queue of the persistent mode (mapped host memory unless noted).
+// Items live in a pool of `cap` slots, freed as each item finishes (in any
+// order); the queue proper is a ring of 2 x cap slot numbers in publishing
+// order, which the kernel's blocks claim from.
 struct Queue {
-    uint32_t cap = 0;                          // ring entries, a power of two
-    BatchItemDev *h_items = nullptr, *d_items = nullptr;
-    unsigned long long *h_pub = nullptr, *d_pub = nullptr;   // items published
+    uint32_t cap = 0;                          // pool slots (and completion entries), a power of two
+    BatchItemDev *h_items = nullptr, *d_items = nullptr;     // the pool
+    uint32_t *h_order = nullptr, *d_order = nullptr;         // queue: pool slot per position [2 cap]
+    unsigned long long *h_pub = nullptr, *d_pub = nullptr;   // positions published
     unsigned *h_mode = nullptr, *d_mode = nullptr;           // QUEUE_HOLD / DRAIN / STOP
-    unsigned long long *h_ring = nullptr, *d_ring = nullptr; // completions [cap][4]
+    unsigned long long *h_ring = nullptr, *d_ring = nullptr; // completions [cap][4], finishing order
     BatchProblemDev *h_problems = nullptr, *d_problems = nullptr;
     unsigned long long *d_counter = nullptr;   // device: claim counter, error flag, live blocks,
                                                // completion count
-    uint64_t done_head = 0;                    // completions taken from the ring
     unsigned *d_done = nullptr;                // device: per launch slot, blocks that ended
     unsigned *h_end = nullptr, *d_end = nullptr;   // per launch slot: {ended, error}
-    uint64_t published = 0;                    // items published so far
-    uint64_t harvested = 0;                    // items below this index are all harvested
-    std::vector<uint64_t> req;                 // per entry: request id of the item
-    std::vector<uint64_t> g;                   // per entry: item index within its request
-    std::vector<uint8_t> state;                // per entry: 0 free, 1 published, 2 harvested
+    uint64_t published = 0;                    // queue positions published
+    uint64_t done_head = 0;                    // completions taken from the ring
+    std::vector<uint32_t> free_slots;          // free pool slots
+    std::vector<uint64_t> req;                 // per pool slot: request id of the item
+    std::vector<uint64_t> g;                   // per pool slot: item index within its request
+    std::vector<uint8_t> state;                // per pool slot: 0 free, 1 published
     unsigned mode = QUEUE_DRAIN;
     bool drained = true;                       // mode was DRAIN since the last launch
 };
@@ -175,6 +179,7 @@ void destroy_server(tmc_server *s)
         cudaStreamDestroy(s->admin);
     cudaFreeHost(s->h_zero);
     cudaFreeHost(s->q.h_items);
+    cudaFreeHost(s->q.h_order);
     cudaFreeHost(s->q.h_pub);
     cudaFreeHost(s->q.h_mode);
     cudaFreeHost(s->q.h_ring);
@@ -471,7 +476,8 @@ int launch_wave(tmc_server *s, Wave &w)
 // ------------------------------------------------------- persistent mode
 
 // Take the finished queue items from the completion ring (in finishing
-// order: only new entries are read), store their probes, decide.
+// order: only new entries are read), store their probes, free their pool
+// slots, decide.
 int harvest_queue(tmc_server *s)
 {
     Queue &Q = s->q;
@@ -480,9 +486,8 @@ int harvest_queue(tmc_server *s)
         unsigned long long *e = Q.h_ring + 4 * (size_t)(Q.done_head & (Q.cap - 1));
         if (__atomic_load_n(&e[3], __ATOMIC_ACQUIRE) == 0)
             break;
-        const uint64_t i = e[2];
-        const uint32_t slot = (uint32_t)(i & (Q.cap - 1));
-        if (i < Q.harvested || i >= Q.published || Q.state[slot] != 1) {
+        const uint64_t slot = e[2];
+        if (slot >= Q.cap || Q.state[slot] != 1) {
             set_error_text("server queue: completion entry for an item not in flight");
             return TMC_E_STATE;
         }
@@ -499,12 +504,9 @@ int harvest_queue(tmc_server *s)
         // free for a later completion, which comes only after more publishing
         __atomic_store_n(&e[3], 0ull, __ATOMIC_RELAXED);
         ++Q.done_head;
-        Q.state[slot] = 2;
+        Q.state[slot] = 0;
+        Q.free_slots.push_back((uint32_t)slot);
         touched.push_back(q.id);
-    }
-    while (Q.harvested < Q.published && Q.state[Q.harvested & (Q.cap - 1)] == 2) {
-        Q.state[Q.harvested & (Q.cap - 1)] = 0;
-        ++Q.harvested;
     }
     std::sort(touched.begin(), touched.end());
     touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
@@ -516,22 +518,26 @@ int harvest_queue(tmc_server *s)
     return TMC_OK;
 }
 
-// Publish pending items into free ring entries, keeping at most
+// Publish pending items into free pool slots, keeping at most
 // inflight_items published and unfinished (so a new request's first round
-// waits behind at most that many items), then release the new count.
+// waits behind at most that many items), then release the new count.  A
+// queue position is reused 2 x cap positions later, when at least cap more
+// items have finished, all claimed after it.
 void publish_queue(tmc_server *s)
 {
     Queue &Q = s->q;
-    const uint64_t budget = s->cfg.inflight_items ? s->cfg.inflight_items : 2ull * (uint64_t)s->grid;
-    const uint64_t room_ring = Q.cap - (Q.published - Q.harvested);
-    const uint64_t room = s->inflight < budget ? std::min<uint64_t>(budget - s->inflight, room_ring) : 0;
+    const uint64_t budget = std::min<uint64_t>(
+        Q.cap, s->cfg.inflight_items ? s->cfg.inflight_items : 2ull * (uint64_t)s->grid);
+    const uint64_t room = s->inflight < budget ? std::min<uint64_t>(budget - s->inflight, Q.free_slots.size()) : 0;
     const uint32_t n = take_pending(s, room, budget, [&](const BatchItemDev &it, uint64_t id, uint64_t g) {
-        const uint64_t i = Q.published++;
-        const uint32_t slot = (uint32_t)(i & (Q.cap - 1));
+        const uint32_t slot = Q.free_slots.back();
+        Q.free_slots.pop_back();
         Q.h_items[slot] = it;
         Q.req[slot] = id;
         Q.g[slot] = g;
         Q.state[slot] = 1;
+        Q.h_order[Q.published & (2 * Q.cap - 1)] = slot;
+        ++Q.published;
     });
     if (n) {
         s->inflight += n;
@@ -554,6 +560,7 @@ int launch_persistent(tmc_server *s, Wave &w)
     a.error = reinterpret_cast<unsigned *>(Q.d_counter + 1);
     a.done_ring = Q.d_ring;
     a.q_items = Q.d_items;
+    a.q_order = Q.d_order;
     a.q_published = Q.d_pub;
     a.q_mode = Q.d_mode;
     a.q_live = reinterpret_cast<unsigned *>(Q.d_counter + 2);
@@ -611,7 +618,7 @@ int progress_persistent(tmc_server *s)
     publish_queue(s);
     // a launch is needed when work is queued and no launch runs, or when the
     // running ones may be ending (the mode was DRAIN since they started)
-    if (Q.published > Q.harvested && (running == 0 || (Q.drained && mode == QUEUE_HOLD))) {
+    if (s->inflight > 0 && (running == 0 || (Q.drained && mode == QUEUE_HOLD))) {
         const uint32_t cap = s->cfg.waves ? s->cfg.waves : DEFAULT_WAVES;
         for (Wave &w : s->waves) {
             if (running >= cap)
@@ -773,6 +780,9 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
         Q.req.assign(Q.cap, 0);
         Q.g.assign(Q.cap, 0);
         Q.state.assign(Q.cap, 0);
+        Q.free_slots.resize(Q.cap);
+        for (uint32_t i = 0; i < Q.cap; ++i)
+            Q.free_slots[i] = Q.cap - 1 - i;
         auto mapped = [&](auto **h, auto **d, size_t bytes) {
             cudaError_t r = cudaHostAlloc(reinterpret_cast<void **>(h), bytes, cudaHostAllocMapped);
             if (r == cudaSuccess) {
@@ -782,6 +792,8 @@ int tmc_server_create(tmc_server **out, const tmc_server_config *cfg)
             return r;
         };
         e = mapped(&Q.h_items, &Q.d_items, sizeof(BatchItemDev) * Q.cap);
+        if (e == cudaSuccess)
+            e = mapped(&Q.h_order, &Q.d_order, sizeof(uint32_t) * 2 * Q.cap);
         if (e == cudaSuccess)
             e = mapped(&Q.h_pub, &Q.d_pub, sizeof(unsigned long long));
         if (e == cudaSuccess)

@@ -52,7 +52,7 @@ struct __align__(16) OpenItem {    // per buffer, in shared memory
     WalkConsts c;                  // optics of the item's problem
     unsigned long long *g;         // the problem's 128-bit global tally
     unsigned long long id_first;   // photon id of the item's first photon
-    unsigned long long qidx;       // queue mode: the item's queue index
+    unsigned long long qidx;       // queue mode: the item's pool slot
     unsigned long long idle_since; // queue mode: first failed claim of this sequence (ns)
     unsigned long long next_poll;  // queue mode: no poll of the published count before (ns)
     uint32_t problem;              // the item's problem
