@@ -132,12 +132,17 @@ def test_split_ranges_add_up(tmc_mod):
     assert s1 + s2 == s0
 
 
-def test_carry_paths_128bit(tmc_mod, oracle_mod):
-    """One block, one shell, high albedo: the block's 64-bit shared sums wrap
-    (sum of w ~ 6.6e7 weight units = 3.9 * 2^64 fixed-point units, sum of w^2
-    ~ 1.9 * 2^64), so the in-kernel carries and the 128-bit flush are all
-    exercised."""
-    optics = dict(shells=1, microns_per_shell=50.0, mu_a=0.1, mu_s=400.0)
+@pytest.mark.parametrize("shells,mps", [(1, 50.0), (1001, 1e7)])
+def test_carry_paths_128bit(tmc_mod, oracle_mod, shells, mps):
+    """One block, high albedo, every deposit in shell 0 (one shell, or 1001
+    shells of 10 m): the shell's sums reach several 2^64 fixed-point units
+    (sum of w ~ 6.6e7 weight units = 3.9 * 2^64, sum of w^2 ~ 1.9 * 2^64).
+    With one shell the kernel keeps a histogram per warp, which each warp adds
+    into the global tally every 2^18 lane steps (a lane walks ~1.9e6 steps
+    here, so every warp flushes several times mid-walk); with 1001 shells it
+    keeps one per block, whose 64-bit shared sums wrap and carry into the
+    global high words.  Both must equal the oracle bit for bit."""
+    optics = dict(shells=shells, microns_per_shell=mps, mu_a=0.1, mu_s=400.0)
     n = 16384
     tmc_mod.set_plain_launch(256, 1, 1)
     got, steps = gpu_fx(tmc_mod, n, seed=9, **optics)

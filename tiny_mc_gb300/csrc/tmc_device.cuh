@@ -205,6 +205,15 @@ __device__ __forceinline__ void tally_add(uint32_t *sh_lo, uint32_t *sh_hi,
     }
 }
 
+// tally_add for a 64-bit sum that cannot wrap (the caller bounds it): the
+// low word's carry goes into the high word, whose old value is not needed.
+__device__ __forceinline__ void tally_add_nowrap(uint32_t *sh_lo, uint32_t *sh_hi, uint32_t lo, uint32_t hi)
+{
+    const uint32_t old = atomicAdd(sh_lo, lo);
+    hi += (old + lo < old) ? 1u : 0u;
+    atomicAdd(sh_hi, hi);
+}
+
 // Flush a 64-bit partial sum into a 128-bit global tally.
 __device__ __forceinline__ void flush128(unsigned long long *g_lo, unsigned long long *g_hi,
                                          unsigned long long v)

@@ -82,7 +82,6 @@ struct PlainLaunch {
     int max_blocks;     // 0 = no cap on the grid
 };
 cudaError_t launch_plain(const PlainLaunch &L, const DeviceCtx &ctx, cudaStream_t stream);
-size_t plain_smem_bytes(uint32_t shells, int block);
 
 // FP64 finalisation on the device (tmc_api.cu).
 cudaError_t launch_tally_to_heat(const tmc_tally *d_tally, uint32_t shells, double c,

@@ -2,11 +2,14 @@
 //
 // Reference path: tiny_mc.c:47-49 calls photon() (photon.c:6-51) once per
 // photon.  Here a persistent grid walks all n photons with the loop in
-// tmc_walk.cuh; each block owns a shared-memory histogram of the problem's
-// shells and adds it to the 128-bit global tally once at the end.  Shell
-// counts whose histogram does not fit in shared memory (params.h's SHELLS is
-// any size in the reference) take the WIDE form: deposits go straight into the
-// 128-bit global tally with 64-bit atomics; the sums are the same integers.
+// tmc_walk.cuh.  Deposits go into shared-memory histograms of the problem's
+// shells: one per warp where that fits without costing occupancy (each warp
+// flushes its own into the 128-bit global tally every 2^18 lane steps and at
+// the end), else one per block, added to the global tally once at the end.
+// Shell counts whose histogram does not fit in shared memory at all
+// (params.h's SHELLS is any size in the reference) take the global form:
+// deposits go straight into the 128-bit global tally with 64-bit atomics.  The
+// sums are the same integers in every form.
 #include <algorithm>
 
 #include "tmc_internal.h"
@@ -26,12 +29,18 @@ struct PlainArgs {
     unsigned long long *steps;   // += photon steps, may be null
 };
 
-template <int BLOCK, class M, bool WIDE>
+// Where a launch keeps its histograms.
+enum class Hist { Block, Warp, Global };
+
+template <int BLOCK, class M, Hist H>
 __global__ void __launch_bounds__(BLOCK) walk_plain(const PlainArgs a)
 {
     extern __shared__ __align__(16) uint32_t smem[];
-    const uint32_t S = WIDE ? 0u : a.c.shells;   // histogram words / 4
-    for (uint32_t s = threadIdx.x; s < 4 * S; s += BLOCK)
+    constexpr bool WIDE = H == Hist::Global;
+    constexpr bool PER_WARP = H == Hist::Warp;
+    const uint32_t S = WIDE ? 0u : a.c.shells;   // words per histogram / 4
+    const uint32_t words = (PER_WARP ? BLOCK / 32 : 1) * 4 * S;
+    for (uint32_t s = threadIdx.x; s < words; s += BLOCK)
         smem[s] = 0;
     __syncthreads();
 
@@ -39,11 +48,14 @@ __global__ void __launch_bounds__(BLOCK) walk_plain(const PlainArgs a)
     src.counter = a.work;
     src.n = a.n_photons;
     src.id_base = a.id_base;
-    uint32_t *my = smem + 4 * S + threadIdx.x;   // ring slot k: my[k * BLOCK]
-    const uint32_t steps =
-        walk_loop<BLOCK, M, GlobalSource<CHUNK>, WIDE>(a.c, src, a.keys, smem, a.tally, my);
+    uint32_t *my = smem + words + threadIdx.x;   // ring slot k: my[k * BLOCK]
+    uint32_t *tally = PER_WARP ? smem + (threadIdx.x / 32) * 4 * S : smem;
+    const uint32_t steps = walk_loop<BLOCK, M, GlobalSource<CHUNK>, WIDE, PER_WARP, REFILL_MIN_SHORT>(
+        a.c, src, a.keys, tally, a.tally, my);
 
-    if constexpr (!WIDE) {
+    if constexpr (PER_WARP) {
+        warp_flush_tally(tally, S, a.tally);
+    } else if constexpr (!WIDE) {
         __syncthreads();
         flush_tally<BLOCK>(smem, S, a.tally);
     }
@@ -54,30 +66,38 @@ __global__ void __launch_bounds__(BLOCK) walk_plain(const PlainArgs a)
     }
 }
 
-size_t plain_smem_bytes(uint32_t shells, int block)
+static size_t plain_smem_bytes(uint32_t shells, int block, Hist h)
 {
-    return (size_t)16 * shells + (size_t)4 * SLOTS * block;
+    const size_t hist = h == Hist::Global ? 0 : (size_t)16 * shells * (h == Hist::Warp ? block / 32 : 1);
+    return hist + (size_t)4 * SLOTS * block;
 }
 
-// Largest shell count whose histogram fits beside a block's ring buffers.
-static uint32_t histogram_max_shells(const DeviceCtx &ctx, int block)
+template <int BLOCK, class M, Hist H>
+static cudaError_t set_smem(size_t smem)
 {
+    return cudaFuncSetAttribute(walk_plain<BLOCK, M, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+// Blocks of walk_plain<BLOCK, M, H> resident per SM with `smem` bytes (0 if
+// it does not fit).
+template <int BLOCK, class M, Hist H>
+static cudaError_t occupancy(const DeviceCtx &ctx, size_t smem, int &per_sm)
+{
+    per_sm = 0;
     const size_t cap = ctx.smem_optin ? ctx.smem_optin : 48 * 1024;
-    const size_t ring = (size_t)4 * SLOTS * block;
-    return cap > ring ? (uint32_t)((cap - ring) / 16) : 0u;
-}
-
-template <int BLOCK, class M, bool WIDE>
-static cudaError_t launch_t(const PlainLaunch &L, const DeviceCtx &ctx, cudaStream_t stream)
-{
-    const size_t smem = plain_smem_bytes(WIDE ? 0u : L.d.shells, BLOCK);
-    auto kern = walk_plain<BLOCK, M, WIDE>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    if (smem > cap)
+        return cudaSuccess;
+    cudaError_t e = set_smem<BLOCK, M, H>(smem);
     if (e != cudaSuccess)
         return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, walk_plain<BLOCK, M, H>, BLOCK, smem);
+}
+
+template <int BLOCK, class M, Hist H>
+static cudaError_t launch_t(const PlainLaunch &L, const DeviceCtx &ctx, int per_sm, cudaStream_t stream)
+{
+    const size_t smem = plain_smem_bytes(L.d.shells, BLOCK, H);
+    cudaError_t e = set_smem<BLOCK, M, H>(smem);
     if (e != cudaSuccess)
         return e;
     if (per_sm < 1)
@@ -103,19 +123,38 @@ static cudaError_t launch_t(const PlainLaunch &L, const DeviceCtx &ctx, cudaStre
     a.tally = reinterpret_cast<unsigned long long *>(L.d_tally);
     a.work = L.d_work;
     a.steps = L.d_steps;
-    kern<<<(unsigned)grid, BLOCK, smem, stream>>>(a);
+    walk_plain<BLOCK, M, H><<<(unsigned)grid, BLOCK, smem, stream>>>(a);
     return cudaGetLastError();
+}
+
+// Per-warp histograms where they fit at the occupancy a per-block histogram
+// would get, else a per-block histogram where it fits, else the global form.
+template <int BLOCK, class M>
+static cudaError_t launch_m(const PlainLaunch &L, const DeviceCtx &ctx, cudaStream_t stream)
+{
+    const uint32_t S = L.d.shells;
+    int warp_sm = 0, block_sm = 0;
+    cudaError_t e = occupancy<BLOCK, M, Hist::Warp>(ctx, plain_smem_bytes(S, BLOCK, Hist::Warp), warp_sm);
+    if (e == cudaSuccess)
+        e = occupancy<BLOCK, M, Hist::Block>(ctx, plain_smem_bytes(S, BLOCK, Hist::Block), block_sm);
+    if (e != cudaSuccess)
+        return e;
+    if (warp_sm >= 1 && warp_sm >= block_sm)
+        return launch_t<BLOCK, M, Hist::Warp>(L, ctx, warp_sm, stream);
+    if (block_sm >= 1)
+        return launch_t<BLOCK, M, Hist::Block>(L, ctx, block_sm, stream);
+    int global_sm = 0;
+    e = occupancy<BLOCK, M, Hist::Global>(ctx, plain_smem_bytes(S, BLOCK, Hist::Global), global_sm);
+    if (e != cudaSuccess)
+        return e;
+    return launch_t<BLOCK, M, Hist::Global>(L, ctx, global_sm, stream);
 }
 
 template <int BLOCK>
 static cudaError_t launch_b(const PlainLaunch &L, const DeviceCtx &ctx, cudaStream_t stream)
 {
-    const bool fast = L.p->math == TMC_MATH_FAST;
-    if (L.d.shells <= histogram_max_shells(ctx, BLOCK))
-        return fast ? launch_t<BLOCK, FastMath, false>(L, ctx, stream)
-                    : launch_t<BLOCK, ExactMath, false>(L, ctx, stream);
-    return fast ? launch_t<BLOCK, FastMath, true>(L, ctx, stream)
-                : launch_t<BLOCK, ExactMath, true>(L, ctx, stream);
+    return L.p->math == TMC_MATH_FAST ? launch_m<BLOCK, FastMath>(L, ctx, stream)
+                                      : launch_m<BLOCK, ExactMath>(L, ctx, stream);
 }
 
 cudaError_t launch_plain(const PlainLaunch &L, const DeviceCtx &ctx, cudaStream_t stream)

@@ -345,11 +345,12 @@ __global__ void __launch_bounds__(BLOCK) walk_stream(const BatchArgs a)
         }
         wait_start = 0;
 
-        // -------- refill once at least two walking lanes are short of the 6
-        // words an iteration may use (or every walking lane is), as walk_loop
+        // -------- refill once REFILL_MIN_SHORT_ITEMS walking lanes are short of the
+        // 6 words an iteration may use (or every walking lane is), as walk_loop
         for (;;) {
             const unsigned low = __ballot_sync(FULL_MASK, alive && (prod - cur) < 6u);
-            if (low == 0 || (__popc(low) < 2 && low != __ballot_sync(FULL_MASK, alive)))
+            if (low == 0 ||
+                (__popc(low) < REFILL_MIN_SHORT_ITEMS && low != __ballot_sync(FULL_MASK, alive)))
                 break;
             if (alive && (prod - cur) <= (uint32_t)(RING - 4)) {
                 const uint4 r = philox4x32_10(blk, 0u, pid_lo, pid_hi, a.keys);

@@ -21,14 +21,19 @@
 //    <= 6 words one iteration reads are fixed offsets from one base.  An
 //    iteration needs >= 6 buffered words (it consumes at most six: step,
 //    four for two tries, roulette); the refill at the top runs once at least
-//    two walking lanes are short (a short lane waits an iteration rather than
-//    make the whole warp pay for a Philox block it alone uses), and then
-//    every lane with room refills, so Philox runs with most lanes active;
-//  * the two tallies of photon.c:30-31 go into a per-block shared-memory
-//    histogram of 64-bit fixed-point sums (sum of w and of w^2, 2^-40 units),
-//    each kept as two 32-bit words updated with native 32-bit shared atomics
-//    (a 64-bit shared atomicAdd is a compare-and-swap loop); a wrap of a
-//    64-bit shared sum carries 2^64 into the 128-bit global tally.
+//    four walking lanes are short (a short lane waits an iteration or two
+//    rather than make the whole warp pay for a Philox block few lanes use),
+//    and then every lane with room refills, so Philox runs with most lanes
+//    active;
+//  * the two tallies of photon.c:30-31 go into a shared-memory histogram of
+//    64-bit fixed-point sums (sum of w and of w^2, 2^-40 units), each kept as
+//    two 32-bit words updated with native 32-bit shared atomics (a 64-bit
+//    shared atomicAdd is a compare-and-swap loop, 4x slower here).  With one
+//    histogram per block, a wrap of a 64-bit shared sum carries 2^64 into the
+//    128-bit global tally.  With one histogram per warp (the plain kernel,
+//    where it fits), the warp adds its histogram into the global tally every
+//    WARP_FLUSH_STEPS lane steps, so its sums cannot wrap and a deposit needs
+//    no wrap check; warps also no longer contend for the same shared words.
 #pragma once
 
 #include "tmc_device.cuh"
@@ -38,6 +43,42 @@ namespace tmc {
 constexpr int RING = 16;        // random words buffered per thread
 constexpr int MIRROR = 6;       // slots 16..21 repeat slots 0..5
 constexpr int SLOTS = RING + MIRROR;
+// The warp runs a Philox refill pass once this many walking lanes are short
+// of words (or every walking lane is).  Measured on the plain walk, 2^30
+// photons of params.h optics: 1 lane 716 ms, 2 lanes 683, 4 lanes 673, 8
+// lanes 681, 16 lanes 709.
+constexpr int REFILL_MIN_SHORT = 4;
+// The same for the batched kernels, whose warps run short of photons at the
+// end of every work item.  Measured on the 4096-problem sweep at 1/64 photon
+// scale: walk_batch (128 threads, 16 items) 1.04e11 photon-steps/s with 2
+// against 1.00e11 with 4; walk_stream (256, 16) 1.006e11 against 0.993e11.
+constexpr int REFILL_MIN_SHORT_ITEMS = 2;
+
+// A warp-private histogram is added into the global tally and cleared each
+// time a lane's step count reaches a multiple of this.  Between two flushes
+// each of the 32 lanes deposits at most WARP_FLUSH_STEPS + 1 times, and a
+// deposit adds at most 2^8 + 1 to a high word (w <= 1, plus the low word's
+// carry), so a high word stays below 32 * 257 * (2^18 + 1) < 2^32: the 64-bit
+// sum never wraps.
+constexpr uint32_t WARP_FLUSH_STEPS = 1u << 18;
+
+// Add a warp's histogram (4 * S words) into the 128-bit global tally and
+// clear it.  Warp-collective.
+__device__ __forceinline__ void warp_flush_tally(uint32_t *tally, uint32_t S, unsigned long long *g)
+{
+    __syncwarp();
+    for (uint32_t s = threadIdx.x & 31u; s < S; s += 32) {
+        flush128(&g[4 * s + 0], &g[4 * s + 1], ((unsigned long long)tally[S + s] << 32) | tally[s]);
+        flush128(&g[4 * s + 2], &g[4 * s + 3],
+                 ((unsigned long long)tally[3 * S + s] << 32) | tally[2 * S + s]);
+        tally[s] = 0;
+        tally[S + s] = 0;
+        tally[2 * S + s] = 0;
+        tally[3 * S + s] = 0;
+    }
+    __syncwarp();
+}
+
 
 // Per-problem constants of photon.c:8-9 (computed on the host in float,
 // exactly as photon.c does) plus the shell count.
@@ -145,8 +186,11 @@ struct SharedSource {
 // block's sum of w in shell probe_shell.  Returns this thread's photon steps.
 // WIDE: no shared histogram (tally unused); every deposit is a 64-bit atomic
 // add into g with the carry into the high word, for shell counts whose
-// histogram does not fit in shared memory.
-template <int BLOCK, class M, class Source, bool WIDE = false>
+// histogram does not fit in shared memory.  PER_WARP: tally is this warp's
+// own histogram, flushed into g every WARP_FLUSH_STEPS lane steps (the caller
+// flushes what is left; probe_wraps unused).
+template <int BLOCK, class M, class Source, bool WIDE = false, bool PER_WARP = false,
+          int MIN_SHORT = REFILL_MIN_SHORT_ITEMS>
 __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
                                               const PhiloxKeys &keys, uint32_t *tally,
                                               unsigned long long *g, uint32_t *my,
@@ -164,10 +208,21 @@ __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
 
     for (;;) {
         // -------- hand new photon ids to lanes whose photon died
-        const unsigned need = __ballot_sync(FULL_MASK, want);
+        // (per-warp histograms: also when a lane's step count reaches a
+        // multiple of WARP_FLUSH_STEPS; checked every iteration, in which a
+        // lane steps at most once)
+        const unsigned need = __ballot_sync(
+            FULL_MASK, want || (PER_WARP && (steps & (WARP_FLUSH_STEPS - 1u)) == 0u));
         if (need) {
+            unsigned want_mask = need;
+            if constexpr (PER_WARP) {
+                if (__any_sync(FULL_MASK, (steps & (WARP_FLUSH_STEPS - 1u)) == 0u))
+                    warp_flush_tally(tally, S, g);
+                want_mask = __ballot_sync(FULL_MASK, want);
+            }
             unsigned long long pid = 0;
-            const bool got = src.next(need, __popc(need & lt_mask), lane, pid);
+            const bool got = want_mask ? src.next(want_mask, __popc(want_mask & lt_mask), lane, pid)
+                                       : false;
             if (want) {
                 want = false;
                 alive = got;
@@ -188,15 +243,16 @@ __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
         }
 
         // -------- refill: an iteration needs >= 6 buffered words (it uses
-        // <= 6).  The warp runs Philox only once at least two walking lanes
-        // are short (or every walking lane is): a refill costs the whole warp
-        // the same issue slots however many lanes take part, so one short
-        // lane waits an iteration instead (the others, using >= 2 words each
-        // per iteration, soon join it).  A fresh photon starts empty and
-        // needs two passes.
+        // <= 6).  The warp runs Philox only once MIN_SHORT walking lanes
+        // are short (or every walking lane is): a refill costs the
+        // whole warp the same issue slots however many lanes take part, so a
+        // short lane waits instead (the others, using >= 2 words each per
+        // iteration, soon join it).  A fresh photon starts empty and needs two
+        // passes.
         for (;;) {
             const unsigned low = __ballot_sync(FULL_MASK, alive && (prod - cur) < 6u);
-            if (low == 0 || (__popc(low) < 2 && low != __ballot_sync(FULL_MASK, alive)))
+            if (low == 0 ||
+                (__popc(low) < MIN_SHORT && low != __ballot_sync(FULL_MASK, alive)))
                 break;
             if (alive && (prod - cur) <= (uint32_t)(RING - 4)) {
                 const uint4 r = philox4x32_10(blk, 0u, pid_lo, pid_hi, keys);
@@ -246,10 +302,16 @@ __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
                 } else {
                     uint32_t *t0 = tally + shell;
                     fx40_split(weight, lo, hi);
-                    tally_add(t0, t0 + S, &g[4 * shell + 1], lo, hi,
-                              shell == probe_shell ? probe_wraps : nullptr);
-                    fx40_split(__fmul_rn(weight, weight), lo, hi);
-                    tally_add(t0 + 2 * S, t0 + 3 * S, &g[4 * shell + 3], lo, hi);
+                    if constexpr (PER_WARP) {
+                        tally_add_nowrap(t0, t0 + S, lo, hi);
+                        fx40_split(__fmul_rn(weight, weight), lo, hi);
+                        tally_add_nowrap(t0 + 2 * S, t0 + 3 * S, lo, hi);
+                    } else {
+                        tally_add(t0, t0 + S, &g[4 * shell + 1], lo, hi,
+                                  shell == probe_shell ? probe_wraps : nullptr);
+                        fx40_split(__fmul_rn(weight, weight), lo, hi);
+                        tally_add(t0 + 2 * S, t0 + 3 * S, &g[4 * shell + 3], lo, hi);
+                    }
                 }
                 weight = M::mul(weight, c.albedo);
                 ++steps;
