@@ -66,15 +66,15 @@ NCU_WALK = {
     "capture": "profiles/walk_plain_fast_2p25photons_ncu_full.txt",
     "sources": ["tiny_mc_gb300/csrc/tmc_device.cuh", "tiny_mc_gb300/csrc/tmc_walk.cuh",
                 "tiny_mc_gb300/csrc/tmc_plain.cu"],
-    "sources_sha256": "f012ddbaba91e908219599fc391eab0d801fd119d4ccd0f38ea35783ef404cff",
+    "sources_sha256": "b4ce523dcf93d7dc6598315124db717c3d49af9206a9f344941034cfa3860628",
     # thread-instructions (predicated on) per photon step
-    "thread_instr_per_step": 232.2,
+    "thread_instr_per_step": 225.5,
     # busy fraction of each pipe
-    "pipes_busy": {"issue_slots": 0.820, "alu": 0.544, "fma": 0.279, "xu_sfu": 0.109,
-                   "shared_wavefronts": 0.515, "dram": 0.0},
+    "pipes_busy": {"issue_slots": 0.829, "alu": 0.551, "fma": 0.340, "xu_sfu": 0.134,
+                   "shared_wavefronts": 0.542, "dram": 0.0},
     # DRAM bytes read + written by one launch (constant and code fetch plus the
-    # 101-shell tally flush; not proportional to the photon count)
-    "dram_bytes_per_launch": 85504,
+    # warps' 101-shell histogram flushes; not proportional to the photon count)
+    "dram_bytes_per_launch": 180992,
 }
 
 
