@@ -66,15 +66,15 @@ NCU_WALK = {
     "capture": "profiles/walk_plain_fast_2p25photons_ncu_full.txt",
     "sources": ["tiny_mc_gb300/csrc/tmc_device.cuh", "tiny_mc_gb300/csrc/tmc_walk.cuh",
                 "tiny_mc_gb300/csrc/tmc_plain.cu"],
-    "sources_sha256": "b4ce523dcf93d7dc6598315124db717c3d49af9206a9f344941034cfa3860628",
+    "sources_sha256": "60efdccc6dc0a868a3da080d59b400576aaf419a07bb1058476d5ceac4b2a1ac",
     # thread-instructions (predicated on) per photon step
     "thread_instr_per_step": 225.5,
     # busy fraction of each pipe
-    "pipes_busy": {"issue_slots": 0.829, "alu": 0.551, "fma": 0.340, "xu_sfu": 0.134,
-                   "shared_wavefronts": 0.542, "dram": 0.0},
+    "pipes_busy": {"issue_slots": 0.827, "alu": 0.550, "fma": 0.340, "xu_sfu": 0.134,
+                   "shared_wavefronts": 0.541, "dram": 0.0},
     # DRAM bytes read + written by one launch (constant and code fetch plus the
     # warps' 101-shell histogram flushes; not proportional to the photon count)
-    "dram_bytes_per_launch": 180992,
+    "dram_bytes_per_launch": 178944,
 }
 
 

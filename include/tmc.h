@@ -246,8 +246,8 @@ int tmc_batch_get_config(const tmc_batch *b, tmc_batch_config *cfg);
 int tmc_batch_autotune(tmc_batch *b, double scale, double max_steps_per_photon, double *best_ms);
 /* Second tuning stage, on the batch itself: takes the fastest configuration
  * of each (kernel, block size) from the last tmc_batch_autotune, at most
- * max_candidates of them in order, times one full run of each and keeps the
- * fastest (a reduced copy cannot rank them: how much the longest single
+ * max_candidates of them (the fastest of each kernel first, then the rest in
+ * order), times one full run of each and keeps the fastest (a reduced copy cannot rank them: how much the longest single
  * photons weigh depends on the batch's size).  Costs max_candidates runs;
  * results do not depend on the configuration.  TMC_E_STATE if autotune has
  * not run.  Not in the reference (it has no batched form). */

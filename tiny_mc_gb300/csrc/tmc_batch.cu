@@ -12,8 +12,10 @@
 //  * each resident block takes the next item from a global counter, zeroes
 //    its shared-memory histogram for that problem's shells, walks the item's
 //    photons with the same loop as the plain kernel (warps claim photons from
-//    a shared-memory counter), then adds the histogram to the problem's
-//    128-bit global tally and takes the next item;
+//    a shared-memory counter; a warp whose lane reaches a multiple of
+//    flush_steps(BLOCK) steps swaps the histogram into the problem's global
+//    tally), then adds what is left to the problem's 128-bit global tally and
+//    takes the next item;
 //  * results are integer tallies keyed by photon id, so each problem's tally
 //    is bit-identical to the plain kernel's for the same photons, whatever
 //    the item split, block size or order;
@@ -42,6 +44,7 @@ __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
     constexpr uint32_t END = 0xffffffffu;
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ uint32_t sh_item, sh_next, sh_probe_wraps;
+    __shared__ unsigned long long sh_probe_acc;
     __shared__ BatchItemDev sh_itm;
     __shared__ BatchProblemDev sh_pr;
     __shared__ unsigned long long sh_qidx;
@@ -77,6 +80,7 @@ __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
             }
             sh_next = 0;
             sh_probe_wraps = 0;
+            sh_probe_acc = 0;
         }
         __syncthreads();
         const uint32_t it = sh_item;
@@ -96,17 +100,20 @@ __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
         unsigned long long *g = a.tally + 4 * pr.tally_offset;
         const uint32_t ps = min(a.probe_shell, S - 1);
         const bool probe = a.item_probe || a.done_ring;
-        const uint32_t steps = walk_loop<BLOCK, M>(pr.c, src, a.keys, smem, g, my,
-                                                   probe ? &sh_probe_wraps : nullptr, ps);
+        const uint32_t steps = walk_loop<BLOCK, M, SharedSource<BATCH_CHUNK>, Hist::Block>(
+            pr.c, src, a.keys, smem, g, my, probe ? &sh_probe_acc : nullptr,
+            probe ? &sh_probe_wraps : nullptr, ps);
 
         __syncthreads();
         flush_tally<BLOCK>(smem, S, g);
-        // this item's own sum of w in the probe shell, 128-bit: the block's
-        // 64-bit shared sum plus its counted 2^64 wraps
-        const unsigned long long probe_lo = ((unsigned long long)smem[S + ps] << 32) | smem[ps];
+        // this item's own sum of w in the probe shell, 128-bit: what the
+        // walk's flushes took from the shell plus what is left in it
+        const unsigned long long rest = ((unsigned long long)smem[S + ps] << 32) | smem[ps];
+        const unsigned long long probe_lo = sh_probe_acc + rest;
+        const uint32_t probe_hi = sh_probe_wraps + (probe_lo < rest ? 1u : 0u);
         if (a.item_probe && threadIdx.x == 0) {
             a.item_probe[2 * (size_t)it] = probe_lo;
-            a.item_probe[2 * (size_t)it + 1] = sh_probe_wraps;
+            a.item_probe[2 * (size_t)it + 1] = probe_hi;
         }
         const unsigned long long tot = warp_sum_u64(steps);
         if ((threadIdx.x & 31u) == 0 && tot)
@@ -116,9 +123,9 @@ __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
         __syncthreads();
         if (a.done_ring && threadIdx.x == 0) {
             if constexpr (QUEUE)
-                publish_item_at(a, sh_qidx, probe_lo, sh_probe_wraps);
+                publish_item_at(a, sh_qidx, probe_lo, probe_hi);
             else
-                publish_item(a, it, probe_lo, sh_probe_wraps);
+                publish_item(a, it, probe_lo, probe_hi);
         }
     }
     if (QUEUE && threadIdx.x == 0)
@@ -779,18 +786,29 @@ int tmc_batch_refine(tmc_batch *b, uint32_t max_candidates, double *best_ms)
         return TMC_E_INVALID;
     if (b->tuned.empty())
         return TMC_E_STATE;
-    // the fastest reduced-copy configuration of each (kernel, block size)
+    // the fastest reduced-copy configuration of each (kernel, block size):
+    // first the fastest of each kernel, so that both kernels are timed on
+    // the batch itself however the reduced copy ranked them, then the rest
+    // in order
     std::vector<std::pair<double, tmc_batch_config>> cand(b->tuned);
     std::stable_sort(cand.begin(), cand.end(),
                      [](const auto &x, const auto &y) { return x.first < y.first; });
     std::vector<tmc_batch_config> pick;
-    for (const auto &c : cand) {
-        bool seen = false;
+    auto add = [&](const tmc_batch_config &c) {
         for (const auto &q : pick)
-            seen = seen || (q.block == c.second.block && q.stream == c.second.stream);
-        if (!seen && pick.size() < max_candidates)
-            pick.push_back(c.second);
-    }
+            if (q.block == c.block && q.stream == c.stream)
+                return;
+        if (pick.size() < max_candidates)
+            pick.push_back(c);
+    };
+    for (uint32_t kernel = 0; kernel < 2; ++kernel)
+        for (const auto &c : cand)
+            if (c.second.stream == kernel) {
+                add(c.second);
+                break;
+            }
+    for (const auto &c : cand)
+        add(c.second);
     const int use_graph = b->cfg.use_graph;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaError_t e = cudaEventCreate(&e0);

@@ -3,9 +3,10 @@
 // Reference path: tiny_mc.c:47-49 calls photon() (photon.c:6-51) once per
 // photon.  Here a persistent grid walks all n photons with the loop in
 // tmc_walk.cuh.  Deposits go into shared-memory histograms of the problem's
-// shells: one per warp where that fits without costing occupancy (each warp
-// flushes its own into the 128-bit global tally every 2^18 lane steps and at
-// the end), else one per block, added to the global tally once at the end.
+// shells: one per warp where that fits without costing occupancy, else one
+// per block; each is added into the 128-bit global tally every flush_steps
+// lane steps (2^18 for a warp's, 2^23 / threads for a block's) and at the
+// end.
 // Shell counts whose histogram does not fit in shared memory at all
 // (params.h's SHELLS is any size in the reference) take the global form:
 // deposits go straight into the 128-bit global tally with 64-bit atomics.  The
@@ -29,16 +30,12 @@ struct PlainArgs {
     unsigned long long *steps;   // += photon steps, may be null
 };
 
-// Where a launch keeps its histograms.
-enum class Hist { Block, Warp, Global };
-
 template <int BLOCK, class M, Hist H>
 __global__ void __launch_bounds__(BLOCK) walk_plain(const PlainArgs a)
 {
     extern __shared__ __align__(16) uint32_t smem[];
-    constexpr bool WIDE = H == Hist::Global;
     constexpr bool PER_WARP = H == Hist::Warp;
-    const uint32_t S = WIDE ? 0u : a.c.shells;   // words per histogram / 4
+    const uint32_t S = H == Hist::Global ? 0u : a.c.shells;   // words per histogram / 4
     const uint32_t words = (PER_WARP ? BLOCK / 32 : 1) * 4 * S;
     for (uint32_t s = threadIdx.x; s < words; s += BLOCK)
         smem[s] = 0;
@@ -50,12 +47,12 @@ __global__ void __launch_bounds__(BLOCK) walk_plain(const PlainArgs a)
     src.id_base = a.id_base;
     uint32_t *my = smem + words + threadIdx.x;   // ring slot k: my[k * BLOCK]
     uint32_t *tally = PER_WARP ? smem + (threadIdx.x / 32) * 4 * S : smem;
-    const uint32_t steps = walk_loop<BLOCK, M, GlobalSource<CHUNK>, WIDE, PER_WARP, REFILL_MIN_SHORT>(
+    const uint32_t steps = walk_loop<BLOCK, M, GlobalSource<CHUNK>, H, REFILL_MIN_SHORT>(
         a.c, src, a.keys, tally, a.tally, my);
 
     if constexpr (PER_WARP) {
         warp_flush_tally(tally, S, a.tally);
-    } else if constexpr (!WIDE) {
+    } else if constexpr (H == Hist::Block) {
         __syncthreads();
         flush_tally<BLOCK>(smem, S, a.tally);
     }

@@ -28,12 +28,12 @@
 //  * the two tallies of photon.c:30-31 go into a shared-memory histogram of
 //    64-bit fixed-point sums (sum of w and of w^2, 2^-40 units), each kept as
 //    two 32-bit words updated with native 32-bit shared atomics (a 64-bit
-//    shared atomicAdd is a compare-and-swap loop, 4x slower here).  With one
-//    histogram per block, a wrap of a 64-bit shared sum carries 2^64 into the
-//    128-bit global tally.  With one histogram per warp (the plain kernel,
-//    where it fits), the warp adds its histogram into the global tally every
-//    WARP_FLUSH_STEPS lane steps, so its sums cannot wrap and a deposit needs
-//    no wrap check; warps also no longer contend for the same shared words.
+//    shared atomicAdd is a compare-and-swap loop, 4x slower here).  The
+//    histogram is one per warp (the plain kernel, where that fits) or one per
+//    block; either way it is added into the 128-bit global tally and cleared
+//    each time one of its lanes' step count reaches a multiple of a bound
+//    (flush_steps), which keeps its 64-bit sums from wrapping, so a deposit
+//    needs no wrap check.
 #pragma once
 
 #include "tmc_device.cuh"
@@ -54,15 +54,27 @@ constexpr int REFILL_MIN_SHORT = 4;
 // against 1.00e11 with 4; walk_stream (256, 16) 1.006e11 against 0.993e11.
 constexpr int REFILL_MIN_SHORT_ITEMS = 2;
 
-// A warp-private histogram is added into the global tally and cleared each
-// time a lane's step count reaches a multiple of this.  Between two flushes
-// each of the 32 lanes deposits at most WARP_FLUSH_STEPS + 1 times, and a
-// deposit adds at most 2^8 + 1 to a high word (w <= 1, plus the low word's
-// carry), so a high word stays below 32 * 257 * (2^18 + 1) < 2^32: the 64-bit
-// sum never wraps.
-constexpr uint32_t WARP_FLUSH_STEPS = 1u << 18;
+// Where a walk keeps its tallies.  Warp: one shared histogram per warp.
+// Block: one per block, shared by its warps.  Global: none; every deposit is
+// a 64-bit atomic add into the 128-bit global tally (shell counts whose
+// histogram does not fit in shared memory).
+enum class Hist { Warp, Block, Global };
 
-// Add a warp's histogram (4 * S words) into the 128-bit global tally and
+// A shared histogram written by `lanes` lanes is added into the global tally
+// and cleared each time one of those lanes' step count reaches a multiple of
+// flush_steps(lanes) (checked at the top of every iteration, in which a lane
+// steps at most once).  Between two flushes each lane deposits at most
+// flush_steps + 1 times, and a deposit adds at most 2^8 + 1 to a high word
+// (w <= 1, plus the low word's carry), so a high word stays below
+// lanes * 257 * (2^23 / lanes + 1) < 2^32: the 64-bit sums never wrap.
+__host__ __device__ constexpr uint32_t flush_steps(uint32_t lanes)
+{
+    return (1u << 23) / lanes;
+}
+static_assert(512ull * 257ull * ((1ull << 23) / 512 + 1) < (1ull << 32), "high word bound");
+static_assert(32ull * 257ull * ((1ull << 23) / 32 + 1) < (1ull << 32), "high word bound");
+
+// Add a warp's own histogram (4 * S words) into the 128-bit global tally and
 // clear it.  Warp-collective.
 __device__ __forceinline__ void warp_flush_tally(uint32_t *tally, uint32_t S, unsigned long long *g)
 {
@@ -79,6 +91,33 @@ __device__ __forceinline__ void warp_flush_tally(uint32_t *tally, uint32_t S, un
     __syncwarp();
 }
 
+// Add a block's histogram into the 128-bit global tally and clear it, by one
+// warp while the others keep depositing: every word is taken with an atomic
+// exchange against zero.  Sums stay exact: a deposit's low-word overflow is
+// carried into a high word by the depositing lane, whichever side of an
+// exchange either add lands on, and every word's content reaches the global
+// tally at one flush or the next.  probe_acc / probe_hi (shared, may be
+// null): the 128-bit running sum of the w words taken from shell
+// probe_shell.  Warp-collective.
+__device__ __forceinline__ void swap_flush_tally(uint32_t *tally, uint32_t S, unsigned long long *g,
+                                                 unsigned long long *probe_acc, uint32_t *probe_hi,
+                                                 uint32_t probe_shell)
+{
+    for (uint32_t s = threadIdx.x & 31u; s < S; s += 32) {
+        const uint32_t lo = atomicExch(&tally[s], 0u);
+        const uint32_t hi = atomicExch(&tally[S + s], 0u);
+        const unsigned long long v = ((unsigned long long)hi << 32) | lo;
+        flush128(&g[4 * s + 0], &g[4 * s + 1], v);
+        if (probe_acc && s == probe_shell && v) {
+            const unsigned long long old = atomicAdd(probe_acc, v);
+            if (old + v < old)
+                atomicAdd(probe_hi, 1u);
+        }
+        const uint32_t lo2 = atomicExch(&tally[2 * S + s], 0u);
+        const uint32_t hi2 = atomicExch(&tally[3 * S + s], 0u);
+        flush128(&g[4 * s + 2], &g[4 * s + 3], ((unsigned long long)hi2 << 32) | lo2);
+    }
+}
 
 // Per-problem constants of photon.c:8-9 (computed on the host in float,
 // exactly as photon.c does) plus the shell count.
@@ -180,21 +219,18 @@ struct SharedSource {
 
 // Walk photons from `src` until it is exhausted and every lane's photon has
 // died.  Warp-collective: all 32 lanes of every warp call it.  tally: the
-// block's shared histogram, 4 * shells words (low and high of sum w, then of
-// sum w^2); g: the problem's global 128-bit tally [shells][4] (receives only
-// carries here).  probe_wraps (may be null): counts the 2^64 wraps of the
-// block's sum of w in shell probe_shell.  Returns this thread's photon steps.
-// WIDE: no shared histogram (tally unused); every deposit is a 64-bit atomic
-// add into g with the carry into the high word, for shell counts whose
-// histogram does not fit in shared memory.  PER_WARP: tally is this warp's
-// own histogram, flushed into g every WARP_FLUSH_STEPS lane steps (the caller
-// flushes what is left; probe_wraps unused).
-template <int BLOCK, class M, class Source, bool WIDE = false, bool PER_WARP = false,
-          int MIN_SHORT = REFILL_MIN_SHORT_ITEMS>
+// shared histogram (H = Warp: this warp's; Block: the block's), 4 * shells
+// words (low and high of sum w, then of sum w^2), flushed into g, the
+// problem's global 128-bit tally [shells][4], every flush_steps lane steps;
+// the caller flushes what is left.  probe_acc / probe_hi (Block only, may be
+// null): receive the w sums those flushes take from shell probe_shell.
+// Returns this thread's photon steps.
+template <int BLOCK, class M, class Source, Hist H, int MIN_SHORT = REFILL_MIN_SHORT_ITEMS>
 __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
                                               const PhiloxKeys &keys, uint32_t *tally,
                                               unsigned long long *g, uint32_t *my,
-                                              uint32_t *probe_wraps = nullptr,
+                                              unsigned long long *probe_acc = nullptr,
+                                              uint32_t *probe_hi = nullptr,
                                               uint32_t probe_shell = 0)
 {
     const uint32_t S = c.shells;
@@ -207,17 +243,21 @@ __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
     uint32_t steps = 0;
 
     for (;;) {
-        // -------- hand new photon ids to lanes whose photon died
-        // (per-warp histograms: also when a lane's step count reaches a
-        // multiple of WARP_FLUSH_STEPS; checked every iteration, in which a
-        // lane steps at most once)
-        const unsigned need = __ballot_sync(
-            FULL_MASK, want || (PER_WARP && (steps & (WARP_FLUSH_STEPS - 1u)) == 0u));
+        // -------- hand new photon ids to lanes whose photon died (shared
+        // histograms: also flush it when a lane's step count reaches a
+        // multiple of the flush bound)
+        constexpr bool SHARED = H != Hist::Global;
+        constexpr uint32_t FLUSH_MASK = flush_steps(H == Hist::Warp ? 32u : (uint32_t)BLOCK) - 1u;
+        const unsigned need = __ballot_sync(FULL_MASK, want || (SHARED && (steps & FLUSH_MASK) == 0u));
         if (need) {
             unsigned want_mask = need;
-            if constexpr (PER_WARP) {
-                if (__any_sync(FULL_MASK, (steps & (WARP_FLUSH_STEPS - 1u)) == 0u))
-                    warp_flush_tally(tally, S, g);
+            if constexpr (SHARED) {
+                if (__any_sync(FULL_MASK, (steps & FLUSH_MASK) == 0u)) {
+                    if constexpr (H == Hist::Warp)
+                        warp_flush_tally(tally, S, g);
+                    else
+                        swap_flush_tally(tally, S, g, probe_acc, probe_hi, probe_shell);
+                }
                 want_mask = __ballot_sync(FULL_MASK, want);
             }
             unsigned long long pid = 0;
@@ -294,7 +334,7 @@ __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
                 const float rr = M::radius_shells(x, y, z, c.spm);
                 const uint32_t shell = __float2uint_rz(fminf(rr, c.last));
                 uint32_t lo, hi;
-                if constexpr (WIDE) {
+                if constexpr (H == Hist::Global) {
                     fx40_split(weight, lo, hi);
                     flush128(&g[4 * shell + 0], &g[4 * shell + 1], ((unsigned long long)hi << 32) | lo);
                     fx40_split(__fmul_rn(weight, weight), lo, hi);
@@ -302,16 +342,9 @@ __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
                 } else {
                     uint32_t *t0 = tally + shell;
                     fx40_split(weight, lo, hi);
-                    if constexpr (PER_WARP) {
-                        tally_add_nowrap(t0, t0 + S, lo, hi);
-                        fx40_split(__fmul_rn(weight, weight), lo, hi);
-                        tally_add_nowrap(t0 + 2 * S, t0 + 3 * S, lo, hi);
-                    } else {
-                        tally_add(t0, t0 + S, &g[4 * shell + 1], lo, hi,
-                                  shell == probe_shell ? probe_wraps : nullptr);
-                        fx40_split(__fmul_rn(weight, weight), lo, hi);
-                        tally_add(t0 + 2 * S, t0 + 3 * S, &g[4 * shell + 3], lo, hi);
-                    }
+                    tally_add_nowrap(t0, t0 + S, lo, hi);
+                    fx40_split(__fmul_rn(weight, weight), lo, hi);
+                    tally_add_nowrap(t0 + 2 * S, t0 + 3 * S, lo, hi);
                 }
                 weight = M::mul(weight, c.albedo);
                 ++steps;
