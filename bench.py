@@ -66,9 +66,9 @@ NCU_WALK = {
     "capture": "profiles/walk_plain_fast_2p25photons_ncu_full.txt",
     "sources": ["tiny_mc_gb300/csrc/tmc_device.cuh", "tiny_mc_gb300/csrc/tmc_walk.cuh",
                 "tiny_mc_gb300/csrc/tmc_plain.cu"],
-    "sources_sha256": "60efdccc6dc0a868a3da080d59b400576aaf419a07bb1058476d5ceac4b2a1ac",
+    "sources_sha256": "ea19d338f68d330bf85235a1a34dc1fde124bf73e8b6288c8c512f1da601432c",
     # thread-instructions (predicated on) per photon step
-    "thread_instr_per_step": 225.5,
+    "thread_instr_per_step": 226.5,
     # busy fraction of each pipe
     "pipes_busy": {"issue_slots": 0.827, "alu": 0.550, "fma": 0.340, "xu_sfu": 0.134,
                    "shared_wavefronts": 0.541, "dram": 0.0},

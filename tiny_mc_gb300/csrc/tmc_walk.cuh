@@ -62,10 +62,14 @@ enum class Hist { Warp, Block, Global };
 
 // A shared histogram written by `lanes` lanes is added into the global tally
 // and cleared each time one of those lanes' step count reaches a multiple of
-// flush_steps(lanes) (checked at the top of every iteration, in which a lane
-// steps at most once).  Between two flushes each lane deposits at most
-// flush_steps + 1 times, and a deposit adds at most 2^8 + 1 to a high word
-// (w <= 1, plus the low word's carry), so a high word stays below
+// flush_steps(lanes), checked at the top of every iteration (in which a lane
+// steps at most once) for every lane that walks a photon or has just lost one
+// (a block's histogram skips lanes left without a photon at the end of a
+// small work item, which would otherwise flush on every iteration).  A lane's
+// count changes only while it walks, so every lane is checked at every
+// multiple it reaches and deposits at most flush_steps + 1 times between two
+// flushes.  A deposit adds at most 2^8 + 1 to a high word (w <= 1, plus the
+// low word's carry), so a high word stays below
 // lanes * 257 * (2^23 / lanes + 1) < 2^32: the 64-bit sums never wrap.
 __host__ __device__ constexpr uint32_t flush_steps(uint32_t lanes)
 {
@@ -248,11 +252,12 @@ __device__ __forceinline__ uint32_t walk_loop(const WalkConsts c, Source &src,
         // multiple of the flush bound)
         constexpr bool SHARED = H != Hist::Global;
         constexpr uint32_t FLUSH_MASK = flush_steps(H == Hist::Warp ? 32u : (uint32_t)BLOCK) - 1u;
-        const unsigned need = __ballot_sync(FULL_MASK, want || (SHARED && (steps & FLUSH_MASK) == 0u));
+        const bool at_bound = (steps & FLUSH_MASK) == 0u && (H == Hist::Warp || alive || want);
+        const unsigned need = __ballot_sync(FULL_MASK, want || (SHARED && at_bound));
         if (need) {
             unsigned want_mask = need;
             if constexpr (SHARED) {
-                if (__any_sync(FULL_MASK, (steps & FLUSH_MASK) == 0u)) {
+                if (__any_sync(FULL_MASK, at_bound)) {
                     if constexpr (H == Hist::Warp)
                         warp_flush_tally(tally, S, g);
                     else
