@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
 {
     constexpr uint32_t END = 0xffffffffu;
     extern __shared__ __align__(16) uint32_t smem[];
-    __shared__ uint32_t sh_item, sh_next, sh_probe_wraps;
+    __shared__ uint32_t sh_item, sh_next, sh_probe_hi;
     __shared__ unsigned long long sh_probe_acc;
     __shared__ BatchItemDev sh_itm;
     __shared__ BatchProblemDev sh_pr;
@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
                 sh_item = (uint32_t)min(atomicAdd(a.item_counter, 1ull), 0xffffffffull);
             }
             sh_next = 0;
-            sh_probe_wraps = 0;
+            sh_probe_hi = 0;
             sh_probe_acc = 0;
         }
         __syncthreads();
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
         const bool probe = a.item_probe || a.done_ring;
         const uint32_t steps = walk_loop<BLOCK, M, SharedSource<BATCH_CHUNK>, Hist::Block>(
             pr.c, src, a.keys, smem, g, my, probe ? &sh_probe_acc : nullptr,
-            probe ? &sh_probe_wraps : nullptr, ps);
+            probe ? &sh_probe_hi : nullptr, ps);
 
         __syncthreads();
         flush_tally<BLOCK>(smem, S, g);
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(BLOCK) walk_batch(const BatchArgs a)
         // walk's flushes took from the shell plus what is left in it
         const unsigned long long rest = ((unsigned long long)smem[S + ps] << 32) | smem[ps];
         const unsigned long long probe_lo = sh_probe_acc + rest;
-        const uint32_t probe_hi = sh_probe_wraps + (probe_lo < rest ? 1u : 0u);
+        const uint32_t probe_hi = sh_probe_hi + (probe_lo < rest ? 1u : 0u);
         if (a.item_probe && threadIdx.x == 0) {
             a.item_probe[2 * (size_t)it] = probe_lo;
             a.item_probe[2 * (size_t)it + 1] = probe_hi;

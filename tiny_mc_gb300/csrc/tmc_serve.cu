@@ -243,8 +243,8 @@ double expected_steps_host(float albedo)
 double batch_rse(const std::vector<unsigned long long> &probe, uint32_t ipb, uint64_t k,
                  double *mean_out)
 {
-    // a batch's value: the exact 128-bit sum of its items' probes (64-bit sum
-    // plus counted 2^64 wraps), converted to weight units once, so it does not
+    // a batch's value: the exact 128-bit sum of its items' probes (low and
+    // high 64-bit words), converted to weight units once, so it does not
     // depend on how many items the batch was split into
     std::vector<double> x(k, 0.0);
     for (uint64_t j = 0; j < k; ++j) {
