@@ -351,8 +351,10 @@ void tmc_server_config_default(tmc_server_config *c);
 int tmc_server_create(tmc_server **out, const tmc_server_config *cfg);
 /* TMC_E_BUSY when no slot is free (the caller queues the request). */
 int tmc_server_submit(tmc_server *s, const tmc_request *r, uint64_t *request_id);
-/* Non-blocking: harvests finished waves, makes stop decisions, launches the
- * next wave on a free stream. */
+/* Non-blocking: harvests finished waves (persistent: the items finished
+ * since the last call), makes stop decisions, and launches the next wave on a
+ * free stream (persistent: publishes the next items to the running launch,
+ * relaunching it if it ended). */
 int tmc_server_progress(tmc_server *s, uint32_t *waves_in_flight, uint32_t *active_requests);
 int tmc_server_poll(tmc_server *s, uint64_t request_id, int *done);
 /* Result of a finished request (then forgotten); tally [shells] may be NULL. */
